@@ -1,0 +1,215 @@
+/*
+ * rh.h — C ABI of the GB300 stochastic myocyte simulator (ryr_hyperactivity_gb300).
+ *
+ * The simulator advances the CRU lattice of one or many independent cells by
+ * one time step per lattice update, then reduces the whole-cell currents and
+ * integrates the membrane model, all on the GPU.  It replaces the per-step
+ * seam of cuda_Cell_Detailed.cu: the `Compute` launch (cuda_Cell_Detailed.cu:217,
+ * :420), the two synchronous device-to-host copies and the host loop that sums
+ * xicat/xinaca/cs and integrates V (:427-739), and the output block (:777-1081).
+ *
+ * Conventions
+ *   - Every call returns an int status: 0 = RH_OK, negative = error.  The text
+ *     of the last error is available from rh_last_error().
+ *   - A handle is single-threaded and not re-entrant; distinct handles may be
+ *     used from different host threads.  The library owns all device memory.
+ *   - No C++ exceptions cross this boundary; plain C types only.
+ *   - Lattice dimensions follow the reference: nx, ny, nz count the ghost
+ *     shell, so a cell has (nx-2)(ny-2)(nz-2) interior CRUs.  Host-side state
+ *     arrays in rh_state_f64 hold interior CRUs only, x fastest:
+ *     index = (i-1) + (nx-2)*((j-1) + (ny-2)*(k-1)); sub-voxel fields are
+ *     8 planes: field[sub*n + index].
+ */
+#ifndef RH_H
+#define RH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RH_ABI_VERSION 1
+
+/* status codes */
+#define RH_OK 0
+#define RH_ERR_ARG -1        /* invalid argument */
+#define RH_ERR_CUDA -2       /* CUDA runtime error */
+#define RH_ERR_NOMEM -3      /* allocation failed */
+#define RH_ERR_NUMERIC -4    /* NaN/Inf detected in a cell (see rh_cell_status) */
+#define RH_ERR_TIMEOUT -5    /* a bounded device wait ran out */
+#define RH_ERR_IO -6         /* checkpoint file error */
+#define RH_ERR_STATE -7      /* call not valid in the current state */
+#define RH_ERR_NOTBUILT -8   /* kernel variant not compiled in */
+
+/* precision modes */
+#define RH_FP64 0   /* every field and operation in FP64 */
+#define RH_MIXED 1  /* lattice fields/rates FP32; V, [Na]i, reductions FP64 */
+
+/* per-cell status bits (rh_cell_status) */
+#define RH_STATUS_NAN 0x1u            /* NaN/Inf in V or a reduced quantity */
+#define RH_STATUS_GAUSS_RETRY 0x2u    /* a Gaussian RyR draw hit the 200-retry cap
+                                         (subroutine_cuda.c:358-361 and siblings) */
+#define RH_STATUS_CI_HIGH 0x4u        /* some ci > 1000 uM at an output step
+                                         (cuda_Cell_Detailed.cu:878-880) */
+#define RH_STATUS_DONE 0x8u           /* the cell reached the end of its protocol */
+
+/* Number of columns of one wholecell record and one linescan row. */
+#define RH_WHOLECELL_COLS 45
+#define RH_LINESCAN_COLS 22
+
+/* Parameters of one cell.  argv[k] refers to the reference command line
+ * (cuda_Cell_Detailed <dev> <name> a3 .. a10). */
+typedef struct {
+  int32_t nx, ny, nz;   /* lattice incl. ghost shell (cuda_Cell_Detailed.cu:80-82) */
+  int32_t nbeats;       /* nbeat (:49) */
+  double pcl_ms;        /* tperid, pacing cycle length (:50) */
+  double clamp_mv;      /* argv[3], clamp voltage (vclamp builds only, :59) */
+  double cjsr_basal;    /* argv[4], initial JSR/NSR load in uM (:92) */
+  double ncx_scale;     /* argv[5]: svncx = 2.5*a5 (:109) */
+  double ku;            /* argv[6]: RyR cp half-activation (:126,:136,:403) */
+  double r1;            /* argv[7]: passed through, unused (reesica.h:14) */
+  double kb;            /* argv[8]: bound-RyR opening scale (:402) */
+  double ica_scale;     /* argv[9]: svica = 0.666*1.2*a9 (:96) */
+  double ku2;           /* argv[10]: RyR CU->OU rate multiplier (:401) */
+  double ikr_scale;     /* multiplies the control IKr prefactor svikr=3 (:138);
+                           forced to 0 under lqt (:128) */
+  double cao_mM;        /* extracellular Ca, Cext (subroutine_cuda.c:24) */
+  int32_t lqt;          /* -Dlqt  (Makefile:9): IKr off */
+  int32_t iso2;         /* -Diso2 (Makefile:16): SERCA x1.75, LCC shifts */
+  int32_t tapsi;        /* -Dtapsi (Makefile:11): SERCA off, cjsr 10 */
+  uint32_t seed;        /* Philox key word 0 (reference: curand seed 18, :377) */
+  uint32_t cell_id;     /* Philox key word 1 */
+  int32_t linescan_jz;  /* z plane of the linescan; -1 = reference's 5 (:972),
+                           clamped to nz-2 when the lattice is thinner */
+} rh_cell_params;
+
+/* Run-wide options. */
+typedef struct {
+  int32_t precision;          /* RH_FP64 or RH_MIXED */
+  int32_t device;             /* CUDA device ordinal */
+  double dt_ms;               /* time step (reference DT 0.025, :51) */
+  int32_t block_size;         /* CRUs per CTA; 0 = use the tuned default */
+  int32_t output_capacity;    /* wholecell records kept per cell between drains */
+  int32_t record_linescan;    /* 1 = keep linescan rows at output steps */
+  int32_t track_stats;        /* 1 = per-beat APD90/EAD/peak-ci/SR-load/sparks */
+  int32_t stats_capacity;     /* beats kept per cell between drains */
+} rh_run_opts;
+
+/* Full FP64 view of one cell's lattice state (caller-owned host arrays of
+ * n = (nx-2)(ny-2)(nz-2) interior CRUs; sub-voxel arrays hold 8*n values).
+ * xire, po, xinaca, xicat, xiup, xileak are the diagnostics of the last
+ * lattice update: written by rh_get_state, ignored by rh_set_state. */
+typedef struct {
+  int32_t n;
+  double *cp, *cs, *cjsr, *cjsrb, *ancx;
+  double *casar, *casarh, *casarj, *casarhj;
+  double *ci, *cnsr, *catf, *cats, *cacal, *casr, *camyo, *mgmyo; /* [8][n] */
+  int32_t *nou, *ncu, *nob, *ncb, *nl, *nspark;
+  int32_t *lcc;                                                    /* [8][n] */
+  double *xire, *po, *xinaca, *xicat;                              /* [n] */
+  double *xiup, *xileak;                                           /* [8][n] */
+} rh_state_f64;
+
+/* Whole-cell (membrane) state of one cell, the host scalars of
+ * cuda_Cell_Detailed.cu:325-371 plus the currents of the last step. */
+typedef struct {
+  double t;             /* ms, accumulated by repeated addition of dt (:1083) */
+  int64_t step;         /* lattice updates done */
+  double v, xnai, xm, xh, xj, xr, xs1, xs2, qks, xtos, ytos, xtof, ytof;
+  double out_ica, out_ncx, out_ina;  /* window accumulators (:774-776) */
+  int64_t sparksum;
+  double csubt, xicatto, xinacato;   /* last reduction (:447-456) */
+  double xina, xiks, xikr, xik1, xinak, xitos, xitof;  /* last currents */
+} rh_membrane;
+
+/* Per-beat statistics of one cell (project-defined detectors). */
+typedef struct {
+  int32_t beat;          /* beat index from 0 */
+  int32_t ead;           /* 1 if an early afterdepolarisation was detected */
+  double apd90_ms;       /* -1 if the AP did not repolarise within the beat */
+  double v_peak;         /* mV */
+  double ci_peak;        /* peak of mean [Ca]i over the beat's output samples, uM */
+  double sr_load;        /* mean cjsr at the last output sample before the stimulus, uM */
+  int32_t sparks;        /* spark onsets in the beat (sum of wholecell column 41) */
+  int32_t pad;
+} rh_beat_stats;
+
+typedef struct rh_sim rh_sim;
+
+/* Defaults: reference's shipped build (cuda_Cell_Detailed.cu:45-145, run.sh:9
+ * "hyper" arguments) on a 64x28x12 lattice. */
+void rh_default_cell_params(rh_cell_params* p);
+void rh_default_run_opts(rh_run_opts* o);
+
+/* Creates a simulator for `ncells` cells and initialises every cell as the
+ * reference's Init kernel does (cuda_Cell_Detailed.cu:1108-1182) plus the
+ * host initial conditions (:349-365). */
+int rh_create(const rh_cell_params* cells, int32_t ncells, const rh_run_opts* opts,
+              rh_sim** out);
+int rh_destroy(rh_sim* sim);
+
+/* Advances every cell that has not finished its protocol by `nsteps` time
+ * steps (one reference loop iteration each, :399-1085).  Cells whose time
+ * reached nbeats*pcl + 2100 ms stop and are flagged RH_STATUS_DONE. */
+int rh_run_steps(rh_sim* sim, int64_t nsteps);
+
+/* Runs until every cell finished its protocol. */
+int rh_run_to_end(rh_sim* sim);
+
+/* Only the lattice update (the Compute kernel, :1187-1692) for every cell,
+ * with the cell's current v, t and [Na]i; no reduction, no V update, t does
+ * not advance.  For single-step parity checks. */
+int rh_lattice_step(rh_sim* sim);
+
+/* Number of cells / interior CRUs of a cell. */
+int rh_num_cells(const rh_sim* sim, int32_t* ncells);
+int rh_cell_size(const rh_sim* sim, int32_t cell, int32_t* n_interior);
+
+/* State transfer (host <-> device) for one cell. */
+int rh_get_state(rh_sim* sim, int32_t cell, rh_state_f64* dst);
+int rh_set_state(rh_sim* sim, int32_t cell, const rh_state_f64* src);
+int rh_get_membrane(rh_sim* sim, int32_t cell, rh_membrane* dst);
+int rh_set_membrane(rh_sim* sim, int32_t cell, const rh_membrane* src);
+
+/* Output records produced since the last drain: wholecell rows of 45 columns
+ * (:1041-1072) and linescan blocks of (nx-2) rows x 22 columns (:974-989).
+ * `*nrec` receives the number of records copied; records beyond `max_rec`
+ * stay queued. */
+int rh_drain_wholecell(rh_sim* sim, int32_t cell, double* rows, int32_t max_rec,
+                       int32_t* nrec);
+int rh_drain_linescan(rh_sim* sim, int32_t cell, double* rows, int32_t max_rec,
+                      int32_t* nrec);
+int rh_drain_stats(rh_sim* sim, int32_t cell, rh_beat_stats* out, int32_t max_rec,
+                   int32_t* nrec);
+
+/* Status bits of a cell (RH_STATUS_*). */
+int rh_cell_status(rh_sim* sim, int32_t cell, uint32_t* status);
+
+/* Binary snapshot of every cell's lattice + membrane state and step counter.
+ * With counter-based random numbers a restored run continues bit-identically. */
+int rh_checkpoint(rh_sim* sim, const char* path);
+int rh_restore(rh_sim* sim, const char* path);
+
+/* Algorithmic HBM bytes moved per interior CRU per lattice update for the
+ * simulator's precision (each persistent field read once, written once). */
+int rh_bytes_per_cru_step(const rh_sim* sim, double* bytes);
+
+/* Device time of the lattice-update kernels, accumulated since the last call
+ * (CUDA events on the simulator's stream); returns launches and milliseconds. */
+int rh_kernel_timing(rh_sim* sim, int64_t* launches, double* ms);
+
+/* Copies the text of the last error into buf (always NUL-terminated). */
+int rh_last_error(const rh_sim* sim, char* buf, size_t n);
+
+/* Formats a wholecell record or one linescan row exactly as the reference's
+ * fprintf calls do (:1041-1072, :974-989).  Returns the string length. */
+int rh_format_wholecell(const double* cols45, char* buf, size_t n);
+int rh_format_linescan(const double* cols22, char* buf, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RH_H */

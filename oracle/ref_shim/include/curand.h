@@ -1,0 +1,1 @@
+/* Empty stand-in: the CUDA declarations the reference needs come from ref_shim.h. */

@@ -1,0 +1,67 @@
+"""Generates the golden fixtures in this directory from the reference program
+compiled for the host (oracle/_ref, built by oracle/build_ref.sh from the
+reference sources).  Run here, where the reference sources exist:
+
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+
+Fixtures (all produced by running the reference's own code):
+  ref_<variant>_wholetest_head.txt   first wholetest_ lines of the run
+  ref_<variant>_linescan_head.txt    first linescan_ blocks of the run
+  ref_full_runs.json                 sha256 and line counts of the complete
+                                     wholetest_/linescan_ files of each run
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+
+# (variant, reference argv a3..a10, lattice/protocol the variant was built with)
+RUNS = {
+    "c1": dict(args=[1.0, 740, 1.0, 3.333, 0.00, 18.0, 0.7, 1],
+               cell=dict(nx=20, ny=10, nz=5, nbeats=2, pcl_ms=400.0, lqt=0, iso2=0,
+                         linescan_jz=-1)),
+    "c1_il": dict(args=[1.0, 740, 1.0, 3.333, 0.00, 18.0, 0.7, 1],
+                  cell=dict(nx=20, ny=10, nz=5, nbeats=2, pcl_ms=400.0, lqt=1, iso2=1,
+                            linescan_jz=-1)),
+    "small_il": dict(args=[1.0, 740, 1.0, 10, 0.00, 1.0, 0.7, 1],
+                     cell=dict(nx=12, ny=9, nz=7, nbeats=1, pcl_ms=1000.0, lqt=1, iso2=1,
+                               linescan_jz=-1)),
+}
+HEAD_WHOLETEST_LINES = 40
+HEAD_LINESCAN_BLOCKS = 6
+
+
+def sha(text: str) -> str:
+    return hashlib.sha256(text.encode()).hexdigest()
+
+
+def main() -> None:
+    meta = {}
+    for variant, spec in RUNS.items():
+        with tempfile.TemporaryDirectory() as d:
+            wt, ls = O.run_ref(variant, spec["args"], d)
+        wt_lines = wt.splitlines(keepends=True)
+        blocks = ls.split("\n\n")
+        with open(os.path.join(HERE, f"ref_{variant}_wholetest_head.txt"), "w") as f:
+            f.write("".join(wt_lines[:HEAD_WHOLETEST_LINES]))
+        with open(os.path.join(HERE, f"ref_{variant}_linescan_head.txt"), "w") as f:
+            f.write("\n\n".join(blocks[:HEAD_LINESCAN_BLOCKS]) + "\n\n")
+        meta[variant] = dict(args=spec["args"], cell=spec["cell"], seed=18,
+                             wholetest_sha256=sha(wt), wholetest_lines=len(wt_lines),
+                             linescan_sha256=sha(ls), linescan_lines=len(ls.splitlines()))
+        print(variant, meta[variant]["wholetest_lines"], "wholetest lines")
+    with open(os.path.join(HERE, "ref_full_runs.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

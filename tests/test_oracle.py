@@ -1,0 +1,91 @@
+"""The CPU oracle against the reference's own outputs.
+
+The fixtures in tests/golden were produced by the reference program itself,
+compiled for the host (oracle/build_ref.sh, tests/golden/make_golden.py).  The
+oracle restatement must reproduce them byte for byte.
+"""
+import hashlib
+import json
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from ryr_hyperactivity_gb300.abi import cell_params
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+META = json.load(open(os.path.join(GOLD, "ref_full_runs.json")))
+
+
+def _params(variant):
+    spec = META[variant]
+    a = spec["args"]
+    return cell_params(clamp_mv=a[0], cjsr_basal=a[1], ncx_scale=a[2], ku=a[3], r1=a[4], kb=a[5],
+                       ica_scale=a[6], ku2=a[7], seed=spec["seed"], **spec["cell"]), spec
+
+
+@pytest.mark.parametrize("variant", ["c1", "c1_il", "small_il"])
+def test_oracle_matches_reference_head(variant):
+    p, spec = _params(variant)
+    want_wt = open(os.path.join(GOLD, f"ref_{variant}_wholetest_head.txt")).read()
+    want_ls = open(os.path.join(GOLD, f"ref_{variant}_linescan_head.txt")).read()
+    nrec = len(want_wt.splitlines())
+    o = O.Oracle(p)
+    _, wc, ls = o.run(nrec * 100 - 99)
+    assert len(wc) == nrec
+    assert O.wholecell_text(wc) == want_wt
+    nblk = want_ls.count("\n\n")
+    assert O.linescan_text(ls[:nblk]) == want_ls
+
+
+@pytest.mark.slow
+def test_oracle_matches_reference_full_run():
+    p, spec = _params("c1")
+    o = O.Oracle(p)
+    _, wc, ls = o.run(10 ** 7, max_rec=spec["wholetest_lines"] + 1)
+    wt = O.wholecell_text(wc)
+    lst = O.linescan_text(ls)
+    assert len(wc) == spec["wholetest_lines"]
+    assert hashlib.sha256(wt.encode()).hexdigest() == spec["wholetest_sha256"]
+    assert hashlib.sha256(lst.encode()).hexdigest() == spec["linescan_sha256"]
+    assert o.done
+
+
+@pytest.mark.skipif(O.ref_binary("small_il") is None, reason="oracle/_ref not built here")
+def test_oracle_matches_reference_build_live():
+    p, spec = _params("small_il")
+    o = O.Oracle(p)
+    _, wc, ls = o.run(3000)
+    with tempfile.TemporaryDirectory() as d:
+        wt, lst = O.run_ref("small_il", spec["args"], d, max_steps=3000)
+    assert O.wholecell_text(wc) == wt
+    assert O.linescan_text(ls) == lst
+
+
+def test_state_roundtrip_and_determinism():
+    p, _ = _params("c1")
+    a = O.Oracle(p)
+    a.run(500)
+    s = a.get_state()
+    m = a.get_membrane()
+    b = O.Oracle(p)
+    b.set_state(s)
+    b.set_membrane(m)
+    a.run(300)
+    b.run(300)
+    sa, sb = a.get_state(), b.get_state()
+    for k in sa.arrays:
+        np.testing.assert_array_equal(sa[k], sb[k], err_msg=k)
+
+
+def test_thread_count_does_not_change_results():
+    p, _ = _params("c1_il")
+    outs = []
+    for nt in (1, 4):
+        o = O.Oracle(p, threads=nt)
+        _, wc, _ = o.run(400)
+        outs.append(wc)
+    O.lib().orc_set_threads(0)
+    np.testing.assert_array_equal(outs[0], outs[1])
