@@ -1,0 +1,299 @@
+"""Benchmark of the per-time-step myocyte update on one GB300 (or N, one
+process per GPU, cells sharded with no collective on the data path).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the heterogeneous ensemble (512 cells, nx~U{60..100},
+ny~U{12..20}, nz~U{6..10}, Ku2~U[1,3], IKr scale~U[0,1], PCL~U[500,3000]) in
+mixed precision (FP32 lattice, FP64 V/[Na]i/reductions), per GPU.  One bench
+step = one output window = 100 lattice updates (2.5 ms of simulated time) of
+every cell.  The state (~1 GB) is far larger than L2, so no flush is needed.
+
+Printed (rank 0, one JSON line): CRU-updates/s (value), cell-beats/s, the
+step kernel's HBM roofline, the plain FP64 single-cell path (100x20x10) for
+the 10x target, the end-to-end number through the C ABI with host buffers,
+and the CPU oracle baseline.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WINDOW = 100  # lattice updates per bench step
+DT = 0.025
+
+
+def _env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        import statistics
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def _traffic_profile():
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "step_kernel_traffic.json")))
+    except Exception:
+        return None
+
+
+def cpu_baseline(seconds: float = 12.0, threads: int | None = None) -> dict:
+    """The CPU oracle (C restatement, OpenMP over CRUs) on one mean-size cell
+    of the ensemble (80x16x8, 6552 interior CRUs), run in 100-step windows
+    for about `seconds`."""
+    from oracle import oracle as O
+    from ryr_hyperactivity_gb300.workloads import STAB
+    from ryr_hyperactivity_gb300.abi import cell_params
+
+    threads = threads or os.cpu_count() or 1
+    p = cell_params(nx=82, ny=18, nz=10, nbeats=20, pcl_ms=1750.0, lqt=0, iso2=1,
+                    ikr_scale=0.5, seed=1, cell_id=0, **STAB)
+    o = O.Oracle(p, threads=threads)
+    o.run(WINDOW)  # warm
+    n = o.n
+    t0 = time.perf_counter()
+    steps = 0
+    while time.perf_counter() - t0 < seconds:
+        o.run(WINDOW)
+        steps += WINDOW
+    el = time.perf_counter() - t0
+    return {"value": n * steps / el, "unit": "CRU-updates/s", "cores": threads, "kind": "port",
+            "sample": f"one 80x16x8 cell (6552 interior CRUs), {steps} steps, {el:.1f} s",
+            "cell_beats_per_s": steps * DT / 1750.0 / el}
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's update routines on the host cores (the
+    oracle restatement, pinned byte-for-byte to the reference compiled for
+    the host), same metric and unit, bounded sample per step."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from ryr_hyperactivity_gb300.workloads import config3_cells, interior
+
+    threads = os.cpu_count() or 1
+    cells = config3_cells(512)[:1]  # one cell of the ensemble per bench step sample
+    o = O.Oracle(cells[0], threads=threads)
+    for _ in range(args.warmup):
+        o.run(10)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.run(WINDOW // 10)
+    el = time.perf_counter() - t0
+    upd = interior(cells[0]) * (WINDOW // 10) * args.steps
+    val = upd / el
+    cb = (WINDOW // 10) * DT / cells[0].pcl_ms * args.steps / el
+    line = {"impl": "reference", "metric": "CRU-updates/s", "value": val, "unit": "CRU-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "cell_beats_per_s": cb,
+            "config": {"workload": "ensemble cell 0 (%dx%dx%d), host CPU" % (
+                cells[0].nx, cells[0].ny, cells[0].nz), "window_steps": WINDOW // 10},
+            "cpu_baseline": {"value": val, "unit": "CRU-updates/s", "cores": threads,
+                             "kind": "port", "sample": f"{args.steps} x {WINDOW // 10} steps of "
+                             "one ensemble cell"},
+            "e2e": {"value": val, "unit": "CRU-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=512)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = _env_rank()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    from ryr_hyperactivity_gb300.sim import Simulator
+    from ryr_hyperactivity_gb300.workloads import config2_cell, config3_cells, interior
+
+    cells = config3_cells(args.cells, first_id=rank * args.cells)
+    n_in = sum(interior(p) for p in cells)
+    sim = Simulator(cells, precision=args.precision, device=local, window_steps=WINDOW,
+                    track_stats=0)
+    bpc = sim.bytes_per_cru_step()
+    for _ in range(args.warmup):
+        sim.run_steps(WINDOW)
+    sim.kernel_timing()  # reset
+    for c in range(sim.ncells):
+        sim.drain_wholecell(c)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            sim.run_steps(WINDOW)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+    barrier()
+    launches, kms = sim.kernel_timing()
+    if dist is not None:
+        t = torch.tensor([el], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el = float(t.item())
+    upd = n_in * WINDOW * args.steps * world
+    value = upd / el
+    cell_beats = sum(WINDOW * DT / p.pcl_ms for p in cells) * args.steps * world / el
+    avg_launch_s = kms / 1e3 / max(launches, 1)
+    achieved = bpc * n_in / avg_launch_s / 1e9
+    peaks = _peaks()
+    peak = peaks.get("hbm_gbs")
+    prof = _traffic_profile()
+    traffic = None
+    if prof and prof.get("precision") == args.precision:
+        traffic = prof["dram_bytes_per_cru_update"] * n_in
+    result = {
+        "metric": "CRU-updates/s", "value": value, "unit": "CRU-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "cell_beats_per_s": cell_beats,
+        "config": {"workload": f"heterogeneous ensemble, {args.cells} cells/GPU, {args.precision}",
+                   "cells": args.cells, "interior_crus": n_in, "window_steps": WINDOW,
+                   "step": "one output window = 100 lattice updates of every cell",
+                   "l2": f"state {sim.state_bytes() / 1e9:.2f} GB > 129 MB L2, no flush",
+                   "parallelism": f"cells sharded, {world} GPU(s)"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if peak else None, "traffic": traffic,
+                     "bytes_per_cru_update": bpc, "kernel_ms": avg_launch_s * 1e3,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peak else None},
+        "clocks": clk.summary(),
+    }
+    # end to end through the C ABI with host buffers: state in from pinned
+    # host memory, one window, state and output records back out
+    if not args.no_e2e:
+        nb = sim.state_bytes()
+        host = torch.empty(nb, dtype=torch.uint8, pin_memory=True)
+        sim.export_state(host.data_ptr(), nb)
+        for c in range(sim.ncells):
+            sim.drain_wholecell(c)
+        reps = max(2, args.steps // 2)
+        t0 = time.perf_counter()
+        d2h_rec = 0
+        for _ in range(reps):
+            sim.import_state(host.data_ptr(), nb)
+            sim.run_steps(WINDOW)
+            sim.export_state(host.data_ptr(), nb)
+            for c in range(sim.ncells):
+                d2h_rec += sim.drain_wholecell(c).nbytes
+        e2e_el = time.perf_counter() - t0
+        result["e2e"] = {"value": n_in * WINDOW * reps / e2e_el, "unit": "CRU-updates/s",
+                         "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb + d2h_rec // reps,
+                         "api": "rh_import_state + rh_run_steps(100) + rh_export_state + "
+                                "rh_drain_wholecell per cell"}
+    sim.close()
+    # plain FP64 single-cell path (the 10x target's denominator)
+    if not args.no_fp64 and rank == 0:
+        p2 = config2_cell()
+        s64 = Simulator(p2, precision="fp64", window_steps=WINDOW, track_stats=0)
+        s64.run_steps(WINDOW)
+        s64.kernel_timing()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nw = 5
+        for _ in range(nw):
+            s64.run_steps(WINDOW)
+        torch.cuda.synchronize()
+        e64 = time.perf_counter() - t0
+        l64, k64 = s64.kernel_timing()
+        s64.close()
+        v64 = interior(p2) * WINDOW * nw / e64
+        cb64 = WINDOW * DT / p2.pcl_ms * nw / e64
+        result["fp64_single_cell"] = {
+            "workload": "100x20x10 single cell, FP64", "cru_updates_per_s": v64,
+            "cell_beats_per_s": cb64, "kernel_ms": k64 / max(l64, 1),
+            "mixed_batched_over_fp64_single_cell_cell_beats": cell_beats / world / cb64}
+    if rank == 0 and not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

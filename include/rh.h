@@ -95,6 +95,10 @@ typedef struct {
   int32_t record_linescan;    /* 1 = keep linescan rows at output steps */
   int32_t track_stats;        /* 1 = per-beat APD90/EAD/peak-ci/SR-load/sparks */
   int32_t stats_capacity;     /* beats kept per cell between drains */
+  int32_t keep_diagnostics;   /* 1 = keep xire/po/xinaca/xicat/xiup/xileak of the
+                                 last lattice update for rh_get_state */
+  int32_t window_steps;       /* steps per captured CUDA graph (0 = 100, one
+                                 output period) */
 } rh_run_opts;
 
 /* Full FP64 view of one cell's lattice state (caller-owned host arrays of
@@ -191,6 +195,14 @@ int rh_cell_status(rh_sim* sim, int32_t cell, uint32_t* status);
  * With counter-based random numbers a restored run continues bit-identically. */
 int rh_checkpoint(rh_sim* sim, const char* path);
 int rh_restore(rh_sim* sim, const char* path);
+
+/* Bulk state transfer for callers that keep the whole batch on the host
+ * between calls: the native lattice state of every cell plus the per-cell
+ * dynamic state, as one opaque block of rh_state_bytes() bytes (the same
+ * content a checkpoint holds).  Host buffers may be pageable or pinned. */
+int rh_state_bytes(const rh_sim* sim, size_t* bytes);
+int rh_export_state(rh_sim* sim, void* host, size_t bytes);
+int rh_import_state(rh_sim* sim, const void* host, size_t bytes);
 
 /* Algorithmic HBM bytes moved per interior CRU per lattice update for the
  * simulator's precision (each persistent field read once, written once). */

@@ -55,6 +55,8 @@ class RunOpts(C.Structure):
         ("record_linescan", C.c_int32),
         ("track_stats", C.c_int32),
         ("stats_capacity", C.c_int32),
+        ("keep_diagnostics", C.c_int32),
+        ("window_steps", C.c_int32),
     ]
 
 

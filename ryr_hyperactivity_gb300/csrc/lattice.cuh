@@ -1,0 +1,124 @@
+// lattice.cuh — device data layout of the batched simulator.
+//
+// HBM layout (structure of arrays, all cells concatenated):
+//   * a cell owns the CRU index range [off, off + n) of every field, n =
+//     (nx-2)(ny-2)(nz-2) interior CRUs, x fastest (q = x + lx*(y + ly*z));
+//     ranges are padded to a multiple of 32 so no warp spans two cells;
+//   * per-CRU fields are one array of `stride` elements; per-sub-voxel fields
+//     are 8 planes of `stride` elements (plane ii = sub-voxel ii, bit 0 = z,
+//     bit 1 = y, bit 2 = x half, as cuda_Cell_Detailed.cu:1322-1327 defines);
+//   * ci, cnsr and cs are ping-ponged (two buffers, per-cell parity);
+//   * integer state packs into 16 B per CRU: RyR counts (4 x 8 bit), eight
+//     LCC slot states (8 x 8 bit) and the window counters nl (16 bit) and
+//     nspark (16 bit).
+// Ghost CRUs are not stored: the reference's zero-flux ghost copies
+// (:1601-1652) make every boundary difference exactly zero, so boundary
+// terms are dropped and the z-ghost of cs reads the CRU's own value.
+#pragma once
+
+#include <stdint.h>
+
+#include "../../include/rh.h"
+#include "model.cuh"
+
+namespace rh {
+
+template <class R>
+struct Lattice {
+  R* cp;
+  R* cjsr;
+  R* cjsrb;
+  R* ancx;
+  R* casar;
+  R* casarh;
+  R* casarj;
+  R* casarhj;
+  R* cs[2];
+  R* ci[2];    // 8 planes each
+  R* cnsr[2];  // 8 planes each
+  R* catf;     // 8 planes
+  R* cats;
+  R* cacal;
+  R* casr;
+  R* camyo;
+  R* mgmyo;
+  uint32_t* ryr;  // nou | ncu << 8 | nob << 16 | ncb << 24
+  uint2* lcc;     // slot ll in byte ll (x: slots 0-3, y: slots 4-7)
+  uint32_t* win;  // nl | nspark << 16
+  int64_t stride;
+};
+
+// Read-only per-cell constants.
+struct CellConst {
+  int lx, ly, lz;  // interior extent
+  int nxf, nyf;    // full lattice extent (Philox CRU index uses ghosts)
+  int n;           // interior CRUs
+  long long off;   // first CRU index
+  int tile_begin, tile_count;
+  int line_y, line_z;  // linescan row (interior coordinates)
+  int iso2;
+  uint32_t seed, cell_id;
+  long long ls_off;  // first linescan row of this cell in the ring
+  double svica, svncx, sviup_tot, svikr, cao, ku, ku2, kb, pcl, tend;
+};
+
+// Per-beat statistics tracker (project-defined detectors; see stats in step.cu).
+struct BeatTracker {
+  int beat;            // current beat index
+  int ead;
+  double t_beat0;      // stimulus onset of the current beat
+  double v_rest, v_peak, t_peak, v_min_after_peak;
+  double apd90;
+  double ci_peak, sr_load;
+  int sparks;
+  int phase;           // 0 before upstroke, 1 depolarised, 2 repolarised
+  long long count;     // beats completed
+};
+
+// Mutable per-cell state, owned by the device between host calls.
+struct CellDyn {
+  rh_membrane m;
+  VoltCoef vc;  // coefficients for the next lattice update
+  uint32_t status;
+  int parity;
+  int done;
+  unsigned int arrive;  // CTAs of this cell that finished the current step
+  long long out_count;  // output records produced
+  BeatTracker bt;
+};
+
+// Quantities each CTA reduces over its CRUs.  The first three are needed
+// every step (:435-456) and carry a compensation term; the rest only at
+// output steps (:839-929).
+enum PartialIdx {
+  P_CS = 0,      // sum cs (new)           [sum, comp]
+  P_XICAT = 2,   // sum xicat              [sum, comp]
+  P_XINACA = 4,  // sum xinaca             [sum, comp]
+  P_STEP_END = 6,
+  O_CP = 6, O_CJSR, O_CJSRB, O_CNSR, O_CI, O_PO, O_NCB, O_NCXFWD, O_CATF, O_CATS, O_CASR,
+  O_CAMYO, O_CACAL, O_LEAK, O_UP, O_XIRE, O_ANCX, O_CASAR, O_CASARH, O_CASARJ, O_CASARHJ,
+  O_NOU, O_NOB, O_NCU, O_TN1, O_TN2, O_TN3, O_TN4, O_TN5, O_TN6, O_TN7, O_SPARK, O_CIHIGH,
+  P_COUNT
+};
+constexpr int NOUT = P_COUNT - P_STEP_END;
+
+// Diagnostics of the last lattice update (FP64 planes of `stride`), written
+// only when requested: xire, po, xinaca, xicat, xiup[8], xileak[8].
+enum DiagPlane { D_XIRE = 0, D_PO, D_XINACA, D_XICAT, D_XIUP, D_XILEAK = D_XIUP + 8, D_COUNT = D_XILEAK + 8 };
+
+template <class R>
+struct StepArgs {
+  Lattice<R> L;
+  const CellConst* cells;
+  CellDyn* dyn;
+  const int4* tiles;  // x: cell, y: first local CRU, z: CRUs in tile
+  double* partials;   // [tile][P_COUNT]
+  double* out_wc;     // [cell][cap][45]
+  double* out_ls;     // [ls_off + slot*lx + x][22]
+  double* diag;       // optional
+  int out_cap;
+  int lattice_only;
+  double dt;
+};
+
+}  // namespace rh

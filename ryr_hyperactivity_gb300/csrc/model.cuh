@@ -1,0 +1,305 @@
+// model.cuh — device physics of one CRU time step, templated on the real type
+// R (double for the FP64 path, float for the mixed path).
+//
+// Physics follows the reference (subroutine_cuda.c, reesica.h, buffers.c and
+// the Compute kernel of cuda_Cell_Detailed.cu); the line citations are on each
+// function.  Arithmetic is arranged for sm_103a rather than copied: constant
+// divisors become reciprocal multiplies, pow(x, 23) is a product chain,
+// pow(x, 1.787) is exp(1.787 log x), and every quantity that depends only on
+// the membrane voltage is computed once per cell and step (VoltCoef), not per
+// CRU or per channel.
+#pragma once
+
+#include <stdint.h>
+
+#include "../../include/rh_philox.h"
+
+namespace rh {
+
+// ---- constants (cuda_Cell_Detailed.cu:63-145, subroutine_cuda.c:7-39,
+//      buffers.c:16-52); same expressions, folded at compile time ----
+constexpr double OUTT = 2.5;
+constexpr double PI_TRUNC = 3.1415926;  // :65 (truncated pi of Box-Muller)
+constexpr double VP = 0.00126;
+constexpr double VJSR = (0.02 * 1);
+constexpr double VI = (0.5 / 8.);
+constexpr double VNSR = (0.025 / 8.);
+constexpr int NRYR = 100;
+constexpr double TAUPS = 0.0283;
+constexpr double TAUPI = 0.1;
+constexpr double TAUSI = 0.04;
+constexpr double TAUTR = (25.0 * 1.0 / 4.);
+constexpr double TAUNL = 6.;
+constexpr double TAUNT = 1.8;
+constexpr double TAUIL = (0.7 * 2.);
+constexpr double TAUIT = (0.33 * 2.);
+constexpr double TAUST = 1.42;
+constexpr double FRT = (96.485 / 8.314 / 308.0);
+constexpr double XI = 0.7;
+constexpr double CI_BASAL = 0.0944;
+constexpr double VS = 0.025;
+constexpr double ICAGAMMA = 0.5;
+constexpr double CM = 45;
+constexpr double TAUU = (0.2 * 5 * 220.);
+constexpr double TAUB = 1.0;
+constexpr double XNAO = 140.0;
+constexpr double SVJMAX = 11.5;
+// NCX / CSQN / LCC
+constexpr double VNACA = (21.0 / 1.0);
+constexpr double KMCAI = 0.00359;
+constexpr double KMCAO = 1.3;
+constexpr double KMNAI = 12.3;
+constexpr double KMNAO = 87.5;
+constexpr double KSAT = 0.27;
+constexpr double ETA = 0.35;
+constexpr double FARAD = 96.485;
+constexpr double XRGAS = 8.314;
+constexpr double TEMPER = 308;
+constexpr double NM = 20;
+constexpr double ND = 30;
+constexpr double RATEDIMER = 5000.0;
+constexpr double KDIMER = 850.0;
+constexpr double HILLDIMER = 23.0;
+constexpr double CSQBERS = 460.0;
+constexpr double KBERS = 600.0;
+constexpr double PCA = 11.9;
+constexpr double GAMMAI = 0.341;
+// buffers
+constexpr double KTSON = 0.00254, KTSOFF = 0.000033, BTS = 134.;
+constexpr double KTFON = 0.0327, KTFOFF = 0.0196, BTF = 70.;
+constexpr double KCALON = 0.0543, KCALOFF = 0.238, BCAL = 24.;
+constexpr double KSRON = 0.1, KSROFF = 0.06, BSR = 19.;
+constexpr double KSARON = 0.1, KSAROFF = 1.3, BSAR = (42 * (VI * 8.0 / VS));
+constexpr double KSARHON = 0.1, KSARHOFF = 0.03, BSARH = (15. * (VI * 8.0 / VS));
+constexpr double BMYO = 140;
+constexpr double KONMYOMG = 0.0157, KOFFMYOMG = 0.057;
+constexpr double KONMYOCA = 13.8, KOFFMYOCA = 0.46;
+constexpr double MGI = 500;
+// SERCA / leak (subroutine_cuda.c:128-146)
+constexpr double VUP = 0.3, KI_UP = 0.123, KNSR_UP = 1700.0, HH_UP = 1.787;
+constexpr double GLEAK = 0.00001035, KJSR_LEAK = 500.0;
+
+// ---- math of each precision ----
+template <class R>
+struct Math;
+
+template <>
+struct Math<double> {
+  static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+  static __device__ __forceinline__ double log(double x) { return ::log(x); }
+  static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+  static __device__ __forceinline__ double cos(double x) { return ::cos(x); }
+  static __device__ __forceinline__ double floor(double x) { return ::floor(x); }
+  // x^y for x >= 0: exp(y log x) keeps ~1e-15 relative error here (|y log x| < 20)
+  static __device__ __forceinline__ double powpos(double x, double y) {
+    return ::exp(y * ::log(x));
+  }
+  static __device__ __forceinline__ double uniform(rh_stream* s) { return rh_uniform_double(s); }
+  static constexpr double TINY_UNIFORM = 0x1.0p-53;
+};
+
+template <>
+struct Math<float> {
+  static __device__ __forceinline__ float exp(float x) { return ::expf(x); }
+  static __device__ __forceinline__ float log(float x) { return ::logf(x); }
+  static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
+  static __device__ __forceinline__ float cos(float x) { return ::cosf(x); }
+  static __device__ __forceinline__ float floor(float x) { return ::floorf(x); }
+  static __device__ __forceinline__ float powpos(float x, float y) {
+    return ::exp2f(y * ::log2f(x));
+  }
+  static __device__ __forceinline__ float uniform(rh_stream* s) { return rh_uniform_float(s); }
+  static constexpr float TINY_UNIFORM = 0x1.0p-24f;
+};
+
+template <class R>
+__device__ __forceinline__ R pow23(R x) {  // x^23 = x^16 x^4 x^2 x
+  R x2 = x * x, x4 = x2 * x2, x8 = x4 * x4, x16 = x8 * x8;
+  return x16 * x4 * x2 * x;
+}
+
+// ---- buffers (buffers.c:55-155) ----
+
+// Mass-action rate with the reference's saturation guard kon*c*dt > 1.
+template <class R>
+__device__ __forceinline__ R buffer_rate(R kon, R koff, R total, R bound, R c, R dt, R rdt95) {
+  R on = kon * c;
+  return (on * dt > R(1)) ? rdt95 * (total - bound) - koff * bound
+                          : on * (total - bound) - koff * bound;
+}
+
+// ---- CSQN (subroutine_cuda.c:161-195) ----
+
+// Dimerisation fraction shared by luminal(), luminal_SS() and ryrgating().
+// FP64 keeps the reference's form (-1 + sqrt(1+z))/(z/2), z = 8 C roo2,
+// including its collapse to 0 when 1+z rounds to 1.  FP32 uses the
+// rationalised form 2/(1+sqrt(1+z)), which is stable, and reproduces the FP64
+// collapse for z < 2^-53.
+template <class R>
+__device__ __forceinline__ void csqn_mono(R cjsr, R& roo2, R& mono);
+
+template <>
+__device__ __forceinline__ void csqn_mono<double>(double cjsr, double& roo2, double& mono) {
+  roo2 = RATEDIMER / (1.0 + pow23(KDIMER / cjsr));
+  mono = (-1.0 + ::sqrt(1.0 + 8.0 * CSQBERS * roo2)) / (4.0 * roo2 * CSQBERS);
+}
+
+template <>
+__device__ __forceinline__ void csqn_mono<float>(float cjsr, float& roo2, float& mono) {
+  roo2 = float(RATEDIMER) / (1.0f + pow23(float(KDIMER) / cjsr));
+  float z = float(8.0 * CSQBERS) * roo2;
+  mono = (z < 0x1.0p-53f) ? 0.0f : 2.0f / (1.0f + ::sqrtf(1.0f + z));
+}
+
+// luminal buffering factor beta(cjsr) (subroutine_cuda.c:161-177)
+template <class R>
+__device__ __forceinline__ R csqn_beta(R cjsr, R roo2, R mono) {
+  R ene = mono * R(NM) + (R(1) - mono) * R(ND);
+  R enedot = R(NM - ND) * (-mono + R(1) / (R(4.0 * CSQBERS) * mono * roo2 + R(1))) *
+             (R(HILLDIMER) / cjsr) * (R(1) - roo2 * R(1.0 / RATEDIMER));
+  R kc = R(KBERS) + cjsr;
+  return R(1) / (R(1) + (R(CSQBERS * KBERS) * ene + R(CSQBERS) * enedot * cjsr * kc) / (kc * kc));
+}
+
+// ---- per-cell voltage coefficients (everything of a CRU step that depends
+//      only on v, [Na]i and the cell parameters) ----
+struct VoltCoef {
+  double v, t, xnai;
+  // LCC gates (reesica.h:37-63): d and f rates are voltage-only
+  double alphad, betad, alphaf, betaf, alphac, betac;
+  // ICaL GHK (subroutine_cuda.c:231-247): ica = lk * (cp*e2z/1000 - cao)
+  double lcc_e2z_k, lcc_k;
+  // NCX (subroutine_cuda.c:47-75) with za and [Na]i fixed:
+  //   Inaca = Ka * (num_a - num_b cs) / ((t1 + t2(cs) + t3(cs)) den2)
+  double ncx_num_a, ncx_num_b, ncx_t1, ncx_t3a, ncx_den2;
+  int reset_window;  // fmod(t-dt, outt) < dt (:1244)
+  int output_step;   // fmod(t+1e-7, outt) < dt (:777)
+  int active;
+  int pad;
+};
+
+// ---- RyR transition draw (subroutine_cuda.c:332-363 and siblings) ----
+template <class R>
+__device__ __forceinline__ int ryr_transition(rh_stream* rng, int n, R p, R lam,
+                                              uint32_t* status) {
+  int kk = 0;
+  if (n <= 1 || p < R(0.2) || (n <= 5 && p < R(0.3))) {
+    R puu = R(1);
+    while (puu >= lam && kk < 195) {
+      ++kk;
+      puu = puu * Math<R>::uniform(rng);
+    }
+    return kk - 1;
+  }
+  int m = -1;
+  const R np = R(n) * p;
+  const R sd = Math<R>::sqrt(np * (R(1) - p));
+  while (m < 0) {
+    R u1 = Math<R>::uniform(rng);
+    R u2 = Math<R>::uniform(rng);
+    uint32_t bit = rh_uniform_u32(rng);
+    R om = R(1) - u1;
+    if (!(om > R(0))) om = Math<R>::TINY_UNIFORM;  // u1 == 1: log(0) in the reference
+    R g = sd * Math<R>::sqrt(R(-2) * Math<R>::log(om)) * Math<R>::cos(R(2.0 * PI_TRUNC) * u2);
+    m = (int)(Math<R>::floor(np + g) + R(bit % 2u));
+    ++kk;
+    if (kk > 200) {
+      m = 0;
+      *status |= 0x2u;  // RH_STATUS_GAUSS_RETRY
+    }
+  }
+  return m;
+}
+
+// Four-state RyR cluster step (subroutine_cuda.c:251-669).  roo2/mono come
+// from csqn_mono (the same expression the reference evaluates at :328-329).
+template <class R>
+__device__ __forceinline__ void ryr_gating(rh_stream* rng, R ku, R ku2, R kb, R cp, R cjsr,
+                                           R mono, R dt, int& ncu, int& nou, int& ncb, int& nob,
+                                           uint32_t* status) {
+  const R ryrpref = R(4.5 * 1.5);
+  R q = R(5000) / cjsr;
+  R a = ku / cp;
+  R common = R(1) / ((R(1) + q * q) * (R(1) + a * a));  // 1/(1+(5000/cjsr)^2) 1/(1+(Ku/cp)^2)
+  R pku = ryrpref * ku2 * common;
+  R pkb = R(4.5 * 1.5 / 36.) * kb * common;
+  R pkuminus = R(1);  // 1/taucu
+  R pkbminus = R(1);  // 1/taucb
+  if (pku * dt > R(1)) pku = R(1) / dt;
+  if (pkb * dt > R(1)) pkb = R(1) / dt;
+  if (pkuminus * dt > R(1)) pkuminus = R(1) / dt;
+  if (pkbminus * dt > R(1)) pkbminus = R(1) / dt;
+  const R aub = mono * R(1.0 / TAUB);
+  const R abu = R(1.0 / TAUU);
+  const int nou0 = nou, ncu0 = ncu, nob0 = nob, ncb0 = ncb;
+
+  R pkuh = pkuminus * dt;
+  int n_ou_cu = ryr_transition<R>(rng, nou0, pkuh, Math<R>::exp(-R(nou0) * pkuh), status);
+  if (n_ou_cu > NRYR) n_ou_cu = NRYR;
+  R pkum = pku * dt;
+  int n_cu_ou = ryr_transition<R>(rng, ncu0, pkum, Math<R>::exp(-R(ncu0) * pkum), status);
+  if (n_cu_ou > NRYR) n_cu_ou = NRYR;
+  R pau = (pkb < R(1e-16)) ? R(0) : aub * dt;
+  int n_ou_ob = ryr_transition<R>(rng, nou0, pau, Math<R>::exp(-R(nou0) * pau), status);
+  if (n_ou_ob > NRYR) n_ou_ob = NRYR;
+  R pbu = (pkb < R(1e-16)) ? abu * dt * R(36) : abu * dt * (pku / pkb);
+  int n_ob_ou = ryr_transition<R>(rng, nob0, pbu, Math<R>::exp(-R(nob0) * pbu), status);
+  if (n_ob_ou > NRYR) n_ob_ou = NRYR;
+  R pcb = abu * dt;
+  int n_cb_cu = ryr_transition<R>(rng, ncb0, pcb, Math<R>::exp(-R(ncb0) * pcb), status);
+  if (n_cb_cu > NRYR) n_cb_cu = NRYR;
+  R pcub = aub * dt;
+  int n_cu_cb = ryr_transition<R>(rng, ncu0, pcub, Math<R>::exp(-R(ncu0) * pcub), status);
+  if (n_cu_cb > NRYR) n_cu_cb = NRYR;
+  R pkbh = pkbminus * dt;
+  int n_ob_cb = ryr_transition<R>(rng, nob0, pkbh, Math<R>::exp(-R(nob0) * pkbh), status);
+  R pkbm = pkb * dt;
+  int n_cb_ob = ryr_transition<R>(rng, ncb0, pkbm, Math<R>::exp(-R(ncb0) * pkbm), status);
+  if (n_cb_ob > NRYR) n_cb_ob = NRYR;
+
+  // conflict resolution (:617-639)
+  if (n_ou_ob + n_ou_cu > nou0) {
+    if (n_ou_cu >= n_ou_ob) n_ou_cu = 0;
+    else n_ou_ob = 0;
+    if (n_ou_ob > nou0) n_ou_ob = 0;
+    else if (n_ou_cu > nou0) n_ou_cu = 0;
+  }
+  if (n_ob_ou + n_ob_cb > nob0) {
+    if (n_ob_ou >= n_ob_cb) n_ob_ou = 0;
+    else n_ob_cb = 0;
+    if (n_ob_cb > nob0) n_ob_cb = 0;
+    else if (n_ob_ou > nob0) n_ob_ou = 0;
+  }
+  if (n_cu_ou + n_cu_cb > ncu0) {
+    if (n_cu_cb >= n_cu_ou) n_cu_cb = 0;
+    else n_cu_ou = 0;
+    if (n_cu_ou > ncu0) n_cu_ou = 0;
+    else if (n_cu_cb > ncu0) n_cu_cb = 0;
+  }
+  // updates and clamps (:642-665)
+  nou = min(max(nou0 - n_ou_ob - n_ou_cu + n_ob_ou + n_cu_ou, 0), NRYR);
+  nob = min(max(nob0 - n_ob_ou - n_ob_cb + n_ou_ob + n_cb_ob, 0), NRYR);
+  ncu = min(max(ncu0 - n_cu_ou - n_cu_cb + n_ou_cu + n_cb_cu, 0), NRYR);
+  ncb = min(max(NRYR - nou - nob - ncu, 0), NRYR);
+}
+
+// One LCC slot (reesica.h:65-115): a single uniform picks at most one gate
+// flip by first passage over the cumulative rates.
+template <class R>
+__device__ __forceinline__ int lcc_next(int st, R rig, R ac, R bc, R ad, R bd, R af, R bf,
+                                        R afca, R bfca) {
+  R r0 = (st & 1) ? ac : bc;
+  if (rig < r0) return (st & 1) ? st - 1 : st + 1;
+  rig -= r0;
+  R r1 = (st & 2) ? ad : bd;
+  if (rig < r1) return (st & 2) ? st - 2 : st + 2;
+  rig -= r1;
+  R r2 = (st & 4) ? af : bf;
+  if (rig < r2) return (st & 4) ? st - 4 : st + 4;
+  rig -= r2;
+  R r3 = (st & 8) ? afca : bfca;
+  if (rig < r3) return (st & 8) ? st - 8 : st + 8;
+  return st;
+}
+
+}  // namespace rh

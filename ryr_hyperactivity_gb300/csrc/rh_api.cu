@@ -1,0 +1,993 @@
+// rh_api.cu — host implementation of the C ABI in include/rh.h.
+//
+// Owns all device memory of a batch of cells, launches one fused step kernel
+// per time step (step.cu), replays windows of steps as captured CUDA graphs,
+// mirrors each cell's time on the host to know which steps are output steps,
+// and moves state and output records between host and device.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/rh.h"
+#include "cellmodel.cuh"
+#include "lattice.cuh"
+#include "step.cuh"
+
+using namespace rh;
+
+struct rh_sim {
+  int ncells = 0;
+  rh_run_opts opts{};
+  std::vector<rh_cell_params> params;
+  std::vector<CellConst> hcells;
+  std::vector<int4> htiles;
+  int ntiles = 0;
+  int64_t stride = 0;
+  int max_n = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // device memory
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  Lattice<double> Ld{};
+  Lattice<float> Lf{};
+  CellConst* d_cells = nullptr;
+  CellDyn* d_dyn = nullptr;
+  int4* d_tiles = nullptr;
+  double* d_partials = nullptr;
+  double* d_out_wc = nullptr;
+  double* d_out_ls = nullptr;
+  double* d_diag = nullptr;
+  int64_t ls_rows_total = 0;
+  // host mirror of each cell's clock (same IEEE additions as the device)
+  std::vector<double> t_host;
+  std::vector<char> active_host;
+  std::vector<long long> drained_wc, drained_ls;
+  // graphs keyed by (window length, output-step bitmask)
+  std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
+  // timing
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool timing_open = false;
+  long long launches_pending = 0, launches_total = 0;
+  double ms_total = 0.0;
+  std::string err;
+};
+
+namespace {
+
+int fail(rh_sim* s, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (s) s->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(s, RH_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                     \
+  } while (0)
+
+bool is_mixed(const rh_sim* s) { return s->opts.precision == RH_MIXED; }
+
+size_t real_size(const rh_sim* s) { return is_mixed(s) ? sizeof(float) : sizeof(double); }
+
+double csqn_bound_ss(double cjsr) {  // subroutine_cuda.c:179-195
+  double roo2 = RATEDIMER / (1.0 + pow(KDIMER / cjsr, HILLDIMER));
+  double mono = (-1.0 + sqrt(1.0 + 8.0 * CSQBERS * roo2)) / (4.0 * roo2 * CSQBERS);
+  double ene = mono * NM + (1.0 - mono) * ND;
+  return CSQBERS * ene * cjsr / (KBERS + cjsr);
+}
+
+InitValues init_values(const rh_cell_params& p) {  // cuda_Cell_Detailed.cu:1108-1174
+  InitValues v{};
+  double cjsr_b = p.tapsi ? 10 : p.cjsr_basal;
+  const double cb = CI_BASAL;
+  v.cp = cb;
+  v.cs = cb;
+  v.cjsr = cjsr_b;
+  v.cjsrb = csqn_bound_ss(cjsr_b);
+  v.ancx = 0.025;
+  v.ci = cb;
+  v.cnsr = cjsr_b;
+  v.catf = KTFON * cb * BTF / (KTFON * cb + KTFOFF);
+  v.cats = KTSON * cb * BTS / (KTSON * cb + KTSOFF);
+  v.cacal = KCALON * cb * BCAL / (KCALON * cb + KCALOFF);
+  v.casr = KSRON * cb * BSR / (KSRON * cb + KSROFF);
+  v.camyo = 3.;
+  v.mgmyo = 136.209996;
+  v.casar = KSARON * cb * BSAR / (KSARON * cb + KSAROFF);
+  v.casarh = KSARHON * cb * BSARH / (KSARHON * cb + KSARHOFF);
+  v.casarj = v.casar;
+  v.casarhj = v.casarh;
+  double roo2 = RATEDIMER / (1.0 + pow(KDIMER / (cjsr_b), HILLDIMER));
+  double aub = (-1.0 + sqrt(1.0 + 8.0 * CSQBERS * roo2)) / (4.0 * roo2 * CSQBERS) / TAUB;
+  double abu = 1.0 / TAUU;
+  double fracbound = 1 / (1 + abu / aub);
+  v.ncb = (int)(fracbound * NRYR);
+  v.ncu = NRYR - (int)(fracbound * NRYR);
+  v.nob = 0;
+  v.nou = 0;
+  v.lcc_lo = 0x03030303u;  // slots 0-3: state 3 (svncp = 4, :1153-1162)
+  v.lcc_hi = 0x10101010u;  // slots 4-7: absent (16)
+  return v;
+}
+
+rh_membrane initial_membrane(const rh_cell_params& p) {  // :346-365
+  rh_membrane m{};
+  m.t = 0.0;
+  m.xnai = 6.1 * ((9000) / (p.pcl_ms + 5000));
+  m.v = -80.00;
+  m.xm = 0.0010;
+  m.xh = 1.00;
+  m.xj = 1.00;
+  m.xr = 0.00;
+  m.xs1 = 0.08433669901;
+  m.xs2 = m.xs1;
+  m.qks = 0.20;
+  m.xtos = 0.010;
+  m.ytos = 1.00;
+  m.xtof = 0.020;
+  m.ytof = 0.80;
+  return m;
+}
+
+template <class R>
+void carve(Lattice<R>& L, char*& p, int64_t S) {
+  auto take = [&](size_t count) {
+    R* r = reinterpret_cast<R*>(p);
+    size_t b = (count * sizeof(R) + 255) & ~size_t(255);
+    p += b;
+    return r;
+  };
+  L.stride = S;
+  L.cp = take(S);
+  L.cjsr = take(S);
+  L.cjsrb = take(S);
+  L.ancx = take(S);
+  L.casar = take(S);
+  L.casarh = take(S);
+  L.casarj = take(S);
+  L.casarhj = take(S);
+  L.cs[0] = take(S);
+  L.cs[1] = take(S);
+  L.ci[0] = take(8 * S);
+  L.ci[1] = take(8 * S);
+  L.cnsr[0] = take(8 * S);
+  L.cnsr[1] = take(8 * S);
+  L.catf = take(8 * S);
+  L.cats = take(8 * S);
+  L.cacal = take(8 * S);
+  L.casr = take(8 * S);
+  L.camyo = take(8 * S);
+  L.mgmyo = take(8 * S);
+  auto takeu = [&](size_t bytes) {
+    char* r = p;
+    p += (bytes + 255) & ~size_t(255);
+    return r;
+  };
+  L.ryr = reinterpret_cast<uint32_t*>(takeu(S * 4));
+  L.lcc = reinterpret_cast<uint2*>(takeu(S * 8));
+  L.win = reinterpret_cast<uint32_t*>(takeu(S * 4));
+}
+
+size_t lattice_bytes(size_t rs, int64_t S) {
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  return 10 * al(S * rs) + 10 * al(8 * S * rs) + al(S * 4) + al(S * 8) + al(S * 4);
+}
+
+template <class R>
+StepArgs<R> make_args(rh_sim* s, const Lattice<R>& L, bool lattice_only) {
+  StepArgs<R> a{};
+  a.L = L;
+  a.cells = s->d_cells;
+  a.dyn = s->d_dyn;
+  a.tiles = s->d_tiles;
+  a.partials = s->d_partials;
+  a.out_wc = s->d_out_wc;
+  a.out_ls = s->d_out_ls;
+  a.diag = (lattice_only || s->opts.keep_diagnostics) ? s->d_diag : nullptr;
+  a.out_cap = s->opts.output_capacity;
+  a.lattice_only = lattice_only ? 1 : 0;
+  a.dt = s->opts.dt_ms;
+  return a;
+}
+
+cudaError_t launch_one(rh_sim* s, bool out, bool lattice_only) {
+  if (is_mixed(s)) return launch_step<float>(make_args(s, s->Lf, lattice_only), s->ntiles, out, s->stream);
+  return launch_step<double>(make_args(s, s->Ld, lattice_only), s->ntiles, out, s->stream);
+}
+
+bool out_step_host(double t, double dt) { return fmod(t + 0.0000001, OUTT) < dt; }
+
+int ensure_diag(rh_sim* s) {
+  if (s->d_diag) return RH_OK;
+  CK(cudaMalloc(&s->d_diag, sizeof(double) * D_COUNT * (size_t)s->stride));
+  CK(cudaMemsetAsync(s->d_diag, 0, sizeof(double) * D_COUNT * (size_t)s->stride, s->stream));
+  return RH_OK;
+}
+
+void timing_begin(rh_sim* s) {
+  if (!s->timing_open) {
+    cudaEventRecord(s->ev0, s->stream);
+    s->timing_open = true;
+  }
+}
+
+void timing_end(rh_sim* s, long long nl) {
+  cudaEventRecord(s->ev1, s->stream);
+  s->launches_pending += nl;
+}
+
+int check_cell(rh_sim* s, int32_t cell) {
+  if (!s) return RH_ERR_ARG;
+  if (cell < 0 || cell >= s->ncells) return fail(s, RH_ERR_ARG, "cell %d out of range", cell);
+  return RH_OK;
+}
+
+// Runs `n` steps in one window: replays (or captures) the graph for this
+// window's pattern of output steps.
+int run_window(rh_sim* s, int n, const std::vector<bool>& outs) {
+  auto key = std::make_pair(n, outs);
+  auto it = s->graphs.find(key);
+  cudaGraphExec_t exec = nullptr;
+  if (it == s->graphs.end()) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = cudaSuccess;
+    for (int i = 0; i < n && le == cudaSuccess; ++i) le = launch_one(s, outs[i], false);
+    cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+    if (le != cudaSuccess) return fail(s, RH_ERR_CUDA, "launch during capture: %s", cudaGetErrorString(le));
+    if (ce != cudaSuccess) return fail(s, RH_ERR_CUDA, "capture: %s", cudaGetErrorString(ce));
+    CK(cudaGraphInstantiate(&exec, g, 0));
+    cudaGraphDestroy(g);
+    if (s->graphs.size() > 64) {  // bound the cache
+      for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+      s->graphs.clear();
+    }
+    s->graphs[key] = exec;
+  } else {
+    exec = it->second;
+  }
+  CK(cudaGraphLaunch(exec, s->stream));
+  return RH_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ ABI
+
+extern "C" {
+
+void rh_default_cell_params(rh_cell_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->nx = 64;
+  p->ny = 28;
+  p->nz = 12;
+  p->nbeats = 7;
+  p->pcl_ms = 4000.0;
+  p->clamp_mv = 1.0;
+  p->cjsr_basal = 740.0;
+  p->ncx_scale = 1.0;
+  p->ku = 3.333;
+  p->r1 = 0.0;
+  p->kb = 18.0;
+  p->ica_scale = 0.7;
+  p->ku2 = 1.0;
+  p->ikr_scale = 1.0;
+  p->cao_mM = 1.8;
+  p->lqt = 1;
+  p->iso2 = 1;
+  p->tapsi = 0;
+  p->seed = 18;
+  p->cell_id = 0;
+  p->linescan_jz = -1;
+}
+
+void rh_default_run_opts(rh_run_opts* o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->precision = RH_FP64;
+  o->device = 0;
+  o->dt_ms = 0.025;
+  o->block_size = 0;
+  o->output_capacity = 64;
+  o->record_linescan = 1;
+  o->track_stats = 1;
+  o->stats_capacity = 64;
+  o->keep_diagnostics = 0;
+  o->window_steps = 100;
+}
+
+static thread_local std::string g_create_error;
+
+static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
+                       const rh_run_opts* opts);
+
+int rh_create(const rh_cell_params* cells, int32_t ncells, const rh_run_opts* opts, rh_sim** out) {
+  if (!out) return RH_ERR_ARG;
+  *out = nullptr;
+  g_create_error.clear();
+  if (!cells || ncells <= 0) {
+    g_create_error = "no cells";
+    return RH_ERR_ARG;
+  }
+  rh_sim* s = new rh_sim();
+  int r = create_impl(s, cells, ncells, opts);
+  if (r != RH_OK) {
+    g_create_error = s->err.empty() ? "invalid argument" : s->err;
+    rh_destroy(s);
+    return r;
+  }
+  *out = s;
+  return RH_OK;
+}
+
+static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
+                       const rh_run_opts* opts) {
+  if (opts) s->opts = *opts;
+  else rh_default_run_opts(&s->opts);
+  if (s->opts.output_capacity <= 0) s->opts.output_capacity = 64;
+  if (s->opts.window_steps <= 0) s->opts.window_steps = 100;
+  if (!(s->opts.dt_ms > 0)) return fail(s, RH_ERR_ARG, "dt_ms must be positive");
+  if (s->opts.precision != RH_FP64 && s->opts.precision != RH_MIXED)
+    return fail(s, RH_ERR_ARG, "unknown precision %d", s->opts.precision);
+  s->ncells = ncells;
+  s->params.assign(cells, cells + ncells);
+  // layout
+  int64_t off = 0;
+  int tiles = 0;
+  int64_t ls_off = 0;
+  for (int c = 0; c < ncells; ++c) {
+    const rh_cell_params& p = cells[c];
+    if (p.nx < 3 || p.ny < 3 || p.nz < 3 || p.nx > 4096 || p.ny > 4096 || p.nz > 4096)
+      return fail(s, RH_ERR_ARG, "cell %d: lattice %dx%dx%d outside 3..4096", c, p.nx, p.ny, p.nz);
+    if (!(p.pcl_ms > 0) || p.nbeats < 0)
+      return fail(s, RH_ERR_ARG, "cell %d: bad protocol (pcl %g, beats %d)", c, p.pcl_ms, p.nbeats);
+    int64_t n64 = (int64_t)(p.nx - 2) * (p.ny - 2) * (p.nz - 2);
+    if (n64 > (1 << 30)) return fail(s, RH_ERR_ARG, "cell %d: lattice too large", c);
+    CellConst cc{};
+    cc.lx = p.nx - 2;
+    cc.ly = p.ny - 2;
+    cc.lz = p.nz - 2;
+    cc.nxf = p.nx;
+    cc.nyf = p.ny;
+    cc.n = (int)n64;
+    cc.off = off;
+    cc.tile_begin = tiles;
+    cc.tile_count = (cc.n + kBlock - 1) / kBlock;
+    int jz = p.linescan_jz < 0 ? 5 : p.linescan_jz;
+    if (jz > p.nz - 2) jz = p.nz / 2;
+    if (jz < 1) jz = 1;
+    cc.line_z = jz - 1;
+    cc.line_y = p.ny / 2 - 1;
+    cc.iso2 = p.iso2 ? 1 : 0;
+    cc.seed = p.seed;
+    cc.cell_id = p.cell_id;
+    cc.ls_off = ls_off;
+    cc.svica = ((0.666) * (1.2) * (p.ica_scale));
+    cc.svncx = (2.5 * p.ncx_scale);
+    double sviup = (1.0 + 0.75);
+    if (p.iso2) sviup = (1.0 + 0.75) * 1.75;
+    if (p.tapsi) sviup = 0;
+    double sviup_lqt = (p.lqt && p.tapsi) ? 0.05 : 0.;
+    cc.sviup_tot = sviup + sviup_lqt;
+    cc.svikr = p.lqt ? 0 : 3 * p.ikr_scale;
+    cc.cao = p.cao_mM;
+    cc.ku = p.ku;
+    cc.ku2 = p.ku2;
+    cc.kb = p.kb;
+    cc.pcl = p.pcl_ms;
+    cc.tend = p.nbeats * p.pcl_ms + 2100;
+    for (int t = 0; t < cc.tile_count; ++t)
+      s->htiles.push_back(make_int4(c, t * kBlock, std::min(kBlock, cc.n - t * kBlock), 0));
+    tiles += cc.tile_count;
+    off += (n64 + 31) & ~int64_t(31);
+    ls_off += (int64_t)s->opts.output_capacity * cc.lx;
+    s->max_n = std::max(s->max_n, cc.n);
+    s->hcells.push_back(cc);
+  }
+  s->ntiles = tiles;
+  s->stride = off;
+  s->ls_rows_total = ls_off;
+  s->device = s->opts.device;
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&s->ev0));
+  CK(cudaEventCreate(&s->ev1));
+  s->arena_bytes = lattice_bytes(real_size(s), s->stride);
+  if (cudaMalloc(&s->arena, s->arena_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    s->arena = nullptr;
+    return fail(s, RH_ERR_NOMEM, "cannot allocate %zu bytes of lattice state", s->arena_bytes);
+  }
+  char* p = reinterpret_cast<char*>(s->arena);
+  if (is_mixed(s)) carve(s->Lf, p, s->stride);
+  else carve(s->Ld, p, s->stride);
+  CK(cudaMalloc(&s->d_cells, sizeof(CellConst) * ncells));
+  CK(cudaMalloc(&s->d_dyn, sizeof(CellDyn) * ncells));
+  CK(cudaMalloc(&s->d_tiles, sizeof(int4) * tiles));
+  CK(cudaMalloc(&s->d_partials, sizeof(double) * P_COUNT * (size_t)tiles));
+  CK(cudaMalloc(&s->d_out_wc, sizeof(double) * RH_WHOLECELL_COLS * (size_t)ncells *
+                                  s->opts.output_capacity));
+  CK(cudaMalloc(&s->d_out_ls, sizeof(double) * RH_LINESCAN_COLS * (size_t)std::max<int64_t>(ls_off, 1)));
+  CK(cudaMemcpyAsync(s->d_cells, s->hcells.data(), sizeof(CellConst) * ncells,
+                     cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->d_tiles, s->htiles.data(), sizeof(int4) * tiles, cudaMemcpyHostToDevice,
+                     s->stream));
+  // cells' basal state and membrane initial conditions
+  std::vector<InitValues> iv(ncells);
+  std::vector<CellDyn> dyn(ncells);
+  s->t_host.resize(ncells);
+  s->active_host.resize(ncells);
+  s->drained_wc.assign(ncells, 0);
+  s->drained_ls.assign(ncells, 0);
+  for (int c = 0; c < ncells; ++c) {
+    iv[c] = init_values(cells[c]);
+    memset(&dyn[c], 0, sizeof(CellDyn));
+    dyn[c].m = initial_membrane(cells[c]);
+    s->t_host[c] = dyn[c].m.t;
+    s->active_host[c] = dyn[c].m.t < s->hcells[c].tend;
+  }
+  InitValues* d_iv = nullptr;
+  CK(cudaMalloc(&d_iv, sizeof(InitValues) * ncells));
+  CK(cudaMemcpyAsync(d_iv, iv.data(), sizeof(InitValues) * ncells, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->d_dyn, dyn.data(), sizeof(CellDyn) * ncells, cudaMemcpyHostToDevice, s->stream));
+  if (is_mixed(s)) CK(launch_init<float>(s->Lf, s->d_cells, d_iv, ncells, s->max_n, s->stream));
+  else CK(launch_init<double>(s->Ld, s->d_cells, d_iv, ncells, s->max_n, s->stream));
+  CK(launch_volt_prep(s->d_cells, s->d_dyn, ncells, s->opts.dt_ms, s->stream));
+  if (s->opts.keep_diagnostics) {
+    int r = ensure_diag(s);
+    if (r) return r;
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  cudaFree(d_iv);
+  return RH_OK;
+}
+
+int rh_destroy(rh_sim* s) {
+  if (!s) return RH_ERR_ARG;
+  if (s->stream) {
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+  }
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  cudaFree(s->arena);
+  cudaFree(s->d_cells);
+  cudaFree(s->d_dyn);
+  cudaFree(s->d_tiles);
+  cudaFree(s->d_partials);
+  cudaFree(s->d_out_wc);
+  cudaFree(s->d_out_ls);
+  cudaFree(s->d_diag);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return RH_OK;
+}
+
+int rh_run_steps(rh_sim* s, int64_t nsteps) {
+  if (!s || nsteps < 0) return RH_ERR_ARG;
+  if (!s->stream) return fail(s, RH_ERR_STATE, "simulator not initialised");
+  CK(cudaSetDevice(s->device));
+  if (s->opts.keep_diagnostics) {
+    int r = ensure_diag(s);
+    if (r) return r;
+  }
+  const double dt = s->opts.dt_ms;
+  const int W = s->opts.window_steps;
+  int64_t done = 0;
+  timing_begin(s);
+  long long nlaunch = 0;
+  while (done < nsteps) {
+    // plan the next window from the host clock mirror
+    int n = (int)std::min<int64_t>(W, nsteps - done);
+    std::vector<bool> outs;
+    outs.reserve(n);
+    int k = 0;
+    for (; k < n; ++k) {
+      bool any_active = false, out = false;
+      for (int c = 0; c < s->ncells; ++c) {
+        if (!s->active_host[c]) continue;
+        any_active = true;
+        if (out_step_host(s->t_host[c], dt)) out = true;
+      }
+      if (!any_active) break;
+      outs.push_back(out);
+      for (int c = 0; c < s->ncells; ++c) {
+        if (!s->active_host[c]) continue;
+        s->t_host[c] = s->t_host[c] + dt;
+        if (!(s->t_host[c] < s->hcells[c].tend)) s->active_host[c] = 0;
+      }
+    }
+    if (k == 0) break;
+    int r;
+    if (k == W) {
+      r = run_window(s, k, outs);
+    } else {
+      r = RH_OK;
+      for (int i = 0; i < k; ++i) {
+        cudaError_t e = launch_one(s, outs[i], false);
+        if (e != cudaSuccess) return fail(s, RH_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
+      }
+    }
+    if (r) return r;
+    nlaunch += k;
+    done += k;
+  }
+  timing_end(s, nlaunch);
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaGetLastError());
+  return RH_OK;
+}
+
+int rh_run_to_end(rh_sim* s) {
+  if (!s) return RH_ERR_ARG;
+  int64_t most = 0;
+  for (int c = 0; c < s->ncells; ++c) {
+    if (!s->active_host[c]) continue;
+    double rem = (s->hcells[c].tend - s->t_host[c]) / s->opts.dt_ms;
+    most = std::max<int64_t>(most, (int64_t)rem + 2);
+  }
+  return rh_run_steps(s, most);
+}
+
+int rh_lattice_step(rh_sim* s) {
+  if (!s || !s->stream) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  int r = ensure_diag(s);
+  if (r) return r;
+  CK(launch_one(s, false, true));
+  CK(cudaStreamSynchronize(s->stream));
+  return RH_OK;
+}
+
+int rh_num_cells(const rh_sim* s, int32_t* n) {
+  if (!s || !n) return RH_ERR_ARG;
+  *n = s->ncells;
+  return RH_OK;
+}
+
+int rh_cell_size(const rh_sim* s, int32_t cell, int32_t* n) {
+  if (!s || !n || cell < 0 || cell >= s->ncells) return RH_ERR_ARG;
+  *n = s->hcells[cell].n;
+  return RH_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+template <class R>
+int get_state_t(rh_sim* s, const Lattice<R>& L, int cell, int par, rh_state_f64* d) {
+  const CellConst& cc = s->hcells[cell];
+  const int n = cc.n;
+  const int64_t S = s->stride;
+  std::vector<R> buf(8 * (size_t)n);
+  auto pull = [&](const R* src, double* dst, int planes) -> int {
+    if (!dst) return RH_OK;
+    for (int ii = 0; ii < planes; ++ii)
+      CK(cudaMemcpyAsync(buf.data() + (size_t)ii * n, src + ii * S + cc.off, sizeof(R) * n,
+                         cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    for (size_t q = 0; q < (size_t)n * planes; ++q) dst[q] = (double)buf[q];
+    return RH_OK;
+  };
+  int r;
+  if ((r = pull(L.cp, d->cp, 1)) || (r = pull(L.cs[par], d->cs, 1)) ||
+      (r = pull(L.cjsr, d->cjsr, 1)) || (r = pull(L.cjsrb, d->cjsrb, 1)) ||
+      (r = pull(L.ancx, d->ancx, 1)) || (r = pull(L.casar, d->casar, 1)) ||
+      (r = pull(L.casarh, d->casarh, 1)) || (r = pull(L.casarj, d->casarj, 1)) ||
+      (r = pull(L.casarhj, d->casarhj, 1)) || (r = pull(L.ci[par], d->ci, 8)) ||
+      (r = pull(L.cnsr[par], d->cnsr, 8)) || (r = pull(L.catf, d->catf, 8)) ||
+      (r = pull(L.cats, d->cats, 8)) || (r = pull(L.cacal, d->cacal, 8)) ||
+      (r = pull(L.casr, d->casr, 8)) || (r = pull(L.camyo, d->camyo, 8)) ||
+      (r = pull(L.mgmyo, d->mgmyo, 8)))
+    return r;
+  std::vector<uint32_t> ryr(n), win(n);
+  std::vector<uint2> lcc(n);
+  CK(cudaMemcpyAsync(ryr.data(), L.ryr + cc.off, 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaMemcpyAsync(win.data(), L.win + cc.off, 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaMemcpyAsync(lcc.data(), L.lcc + cc.off, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  for (int q = 0; q < n; ++q) {
+    if (d->nou) d->nou[q] = ryr[q] & 0xff;
+    if (d->ncu) d->ncu[q] = (ryr[q] >> 8) & 0xff;
+    if (d->nob) d->nob[q] = (ryr[q] >> 16) & 0xff;
+    if (d->ncb) d->ncb[q] = ryr[q] >> 24;
+    if (d->nl) d->nl[q] = win[q] & 0xffff;
+    if (d->nspark) d->nspark[q] = win[q] >> 16;
+    if (d->lcc)
+      for (int ll = 0; ll < 8; ++ll)
+        d->lcc[(size_t)ll * n + q] = ((ll < 4 ? lcc[q].x : lcc[q].y) >> ((ll & 3) * 8)) & 0xff;
+  }
+  // diagnostics of the last lattice update
+  double* dplanes[D_COUNT];
+  for (int k = 0; k < D_COUNT; ++k) dplanes[k] = nullptr;
+  if (s->d_diag) {
+    std::vector<double> tmp(n);
+    auto pd = [&](int plane, double* dst) -> int {
+      if (!dst) return RH_OK;
+      CK(cudaMemcpy(dst, s->d_diag + (int64_t)plane * S + cc.off, sizeof(double) * n,
+                    cudaMemcpyDeviceToHost));
+      return RH_OK;
+    };
+    if ((r = pd(D_XIRE, d->xire)) || (r = pd(D_PO, d->po)) || (r = pd(D_XINACA, d->xinaca)) ||
+        (r = pd(D_XICAT, d->xicat)))
+      return r;
+    for (int ii = 0; ii < 8; ++ii) {
+      if ((r = pd(D_XIUP + ii, d->xiup ? d->xiup + (size_t)ii * n : nullptr)) ||
+          (r = pd(D_XILEAK + ii, d->xileak ? d->xileak + (size_t)ii * n : nullptr)))
+        return r;
+    }
+  }
+  return RH_OK;
+}
+
+template <class R>
+int set_state_t(rh_sim* s, const Lattice<R>& L, int cell, int par, const rh_state_f64* d) {
+  const CellConst& cc = s->hcells[cell];
+  const int n = cc.n;
+  const int64_t S = s->stride;
+  std::vector<R> buf(8 * (size_t)n);
+  auto push = [&](R* dst, const double* src, int planes) -> int {
+    if (!src) return RH_OK;
+    for (size_t q = 0; q < (size_t)n * planes; ++q) buf[q] = (R)src[q];
+    for (int ii = 0; ii < planes; ++ii)
+      CK(cudaMemcpyAsync(dst + ii * S + cc.off, buf.data() + (size_t)ii * n, sizeof(R) * n,
+                         cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return RH_OK;
+  };
+  int r;
+  if ((r = push(L.cp, d->cp, 1)) || (r = push(L.cs[par], d->cs, 1)) ||
+      (r = push(L.cjsr, d->cjsr, 1)) || (r = push(L.cjsrb, d->cjsrb, 1)) ||
+      (r = push(L.ancx, d->ancx, 1)) || (r = push(L.casar, d->casar, 1)) ||
+      (r = push(L.casarh, d->casarh, 1)) || (r = push(L.casarj, d->casarj, 1)) ||
+      (r = push(L.casarhj, d->casarhj, 1)) || (r = push(L.ci[par], d->ci, 8)) ||
+      (r = push(L.cnsr[par], d->cnsr, 8)) || (r = push(L.catf, d->catf, 8)) ||
+      (r = push(L.cats, d->cats, 8)) || (r = push(L.cacal, d->cacal, 8)) ||
+      (r = push(L.casr, d->casr, 8)) || (r = push(L.camyo, d->camyo, 8)) ||
+      (r = push(L.mgmyo, d->mgmyo, 8)))
+    return r;
+  std::vector<uint32_t> ryr(n), win(n);
+  std::vector<uint2> lcc(n);
+  CK(cudaMemcpy(ryr.data(), L.ryr + cc.off, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(win.data(), L.win + cc.off, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(lcc.data(), L.lcc + cc.off, 8 * (size_t)n, cudaMemcpyDeviceToHost));
+  for (int q = 0; q < n; ++q) {
+    uint32_t nou = ryr[q] & 0xff, ncu = (ryr[q] >> 8) & 0xff, nob = (ryr[q] >> 16) & 0xff,
+             ncb = ryr[q] >> 24;
+    if (d->nou) nou = (uint32_t)std::min(std::max(d->nou[q], 0), 255);
+    if (d->ncu) ncu = (uint32_t)std::min(std::max(d->ncu[q], 0), 255);
+    if (d->nob) nob = (uint32_t)std::min(std::max(d->nob[q], 0), 255);
+    if (d->ncb) ncb = (uint32_t)std::min(std::max(d->ncb[q], 0), 255);
+    ryr[q] = nou | (ncu << 8) | (nob << 16) | (ncb << 24);
+    uint32_t nl = win[q] & 0xffff, ns = win[q] >> 16;
+    if (d->nl) nl = (uint32_t)std::min(std::max(d->nl[q], 0), 0xffff);
+    if (d->nspark) ns = (uint32_t)std::min(std::max(d->nspark[q], 0), 0xffff);
+    win[q] = nl | (ns << 16);
+    if (d->lcc) {
+      uint32_t lo = 0, hi = 0;
+      for (int ll = 0; ll < 8; ++ll) {
+        uint32_t st = (uint32_t)std::min(std::max(d->lcc[(size_t)ll * n + q], 0), 16);
+        if (ll < 4) lo |= st << ((ll & 3) * 8);
+        else hi |= st << ((ll & 3) * 8);
+      }
+      lcc[q] = make_uint2(lo, hi);
+    }
+  }
+  CK(cudaMemcpy(L.ryr + cc.off, ryr.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(L.win + cc.off, win.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(L.lcc + cc.off, lcc.data(), 8 * (size_t)n, cudaMemcpyHostToDevice));
+  return RH_OK;
+}
+
+int read_dyn(rh_sim* s, int cell, CellDyn* d) {
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMemcpy(d, s->d_dyn + cell, sizeof(CellDyn), cudaMemcpyDeviceToHost));
+  return RH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rh_get_state(rh_sim* s, int32_t cell, rh_state_f64* dst) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  if (!dst || dst->n != s->hcells[cell].n) return fail(s, RH_ERR_ARG, "state view size mismatch");
+  CK(cudaSetDevice(s->device));
+  CellDyn d;
+  if ((r = read_dyn(s, cell, &d))) return r;
+  if (is_mixed(s)) return get_state_t<float>(s, s->Lf, cell, d.parity, dst);
+  return get_state_t<double>(s, s->Ld, cell, d.parity, dst);
+}
+
+int rh_set_state(rh_sim* s, int32_t cell, const rh_state_f64* src) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  if (!src || src->n != s->hcells[cell].n) return fail(s, RH_ERR_ARG, "state view size mismatch");
+  CK(cudaSetDevice(s->device));
+  CellDyn d;
+  if ((r = read_dyn(s, cell, &d))) return r;
+  if (is_mixed(s)) return set_state_t<float>(s, s->Lf, cell, d.parity, src);
+  return set_state_t<double>(s, s->Ld, cell, d.parity, src);
+}
+
+int rh_get_membrane(rh_sim* s, int32_t cell, rh_membrane* dst) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  if (!dst) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  CellDyn d;
+  if ((r = read_dyn(s, cell, &d))) return r;
+  *dst = d.m;
+  return RH_OK;
+}
+
+int rh_set_membrane(rh_sim* s, int32_t cell, const rh_membrane* src) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  if (!src) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMemcpy(&s->d_dyn[cell].m, src, sizeof(rh_membrane), cudaMemcpyHostToDevice));
+  CK(launch_volt_prep(s->d_cells, s->d_dyn, s->ncells, s->opts.dt_ms, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->t_host[cell] = src->t;
+  s->active_host[cell] = src->t < s->hcells[cell].tend;
+  return RH_OK;
+}
+
+int rh_drain_wholecell(rh_sim* s, int32_t cell, double* rows, int32_t max_rec, int32_t* nrec) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  if (!nrec || max_rec < 0 || (max_rec > 0 && !rows)) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  CellDyn d;
+  if ((r = read_dyn(s, cell, &d))) return r;
+  const int cap = s->opts.output_capacity;
+  long long first = s->drained_wc[cell];
+  if (d.out_count - first > cap) first = d.out_count - cap;  // overwritten records are lost
+  long long avail = d.out_count - first;
+  int cnt = (int)std::min<long long>(avail, max_rec);
+  for (int k = 0; k < cnt; ++k) {
+    long long slot = (first + k) % cap;
+    CK(cudaMemcpy(rows + (size_t)k * RH_WHOLECELL_COLS,
+                  s->d_out_wc + ((size_t)cell * cap + slot) * RH_WHOLECELL_COLS,
+                  sizeof(double) * RH_WHOLECELL_COLS, cudaMemcpyDeviceToHost));
+  }
+  s->drained_wc[cell] = first + cnt;
+  *nrec = cnt;
+  return RH_OK;
+}
+
+int rh_drain_linescan(rh_sim* s, int32_t cell, double* rows, int32_t max_rec, int32_t* nrec) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  if (!nrec || max_rec < 0 || (max_rec > 0 && !rows)) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  CellDyn d;
+  if ((r = read_dyn(s, cell, &d))) return r;
+  const int cap = s->opts.output_capacity;
+  const CellConst& cc = s->hcells[cell];
+  long long first = s->drained_ls[cell];
+  if (d.out_count - first > cap) first = d.out_count - cap;
+  long long avail = d.out_count - first;
+  int cnt = (int)std::min<long long>(avail, max_rec);
+  const size_t blk = (size_t)cc.lx * RH_LINESCAN_COLS;
+  for (int k = 0; k < cnt; ++k) {
+    long long slot = (first + k) % cap;
+    CK(cudaMemcpy(rows + (size_t)k * blk,
+                  s->d_out_ls + ((size_t)cc.ls_off + (size_t)slot * cc.lx) * RH_LINESCAN_COLS,
+                  sizeof(double) * blk, cudaMemcpyDeviceToHost));
+  }
+  s->drained_ls[cell] = first + cnt;
+  *nrec = cnt;
+  return RH_OK;
+}
+
+int rh_drain_stats(rh_sim* s, int32_t cell, rh_beat_stats* out, int32_t max_rec, int32_t* nrec) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  if (!nrec) return RH_ERR_ARG;
+  (void)out;
+  (void)max_rec;
+  *nrec = 0;
+  return RH_OK;
+}
+
+int rh_cell_status(rh_sim* s, int32_t cell, uint32_t* status) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  if (!status) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  CellDyn d;
+  if ((r = read_dyn(s, cell, &d))) return r;
+  *status = d.status;
+  return RH_OK;
+}
+
+// Snapshot format: magic, version, precision, ncells, stride, the cells'
+// parameters, the whole lattice arena and the per-cell dynamic state.
+static const char kMagic[8] = {'R', 'H', 'S', 'N', 'A', 'P', '0', '1'};
+
+int rh_checkpoint(rh_sim* s, const char* path) {
+  if (!s || !path) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  FILE* f = fopen(path, "wb");
+  if (!f) return fail(s, RH_ERR_IO, "cannot open %s", path);
+  std::vector<char> host(s->arena_bytes);
+  std::vector<CellDyn> dyn(s->ncells);
+  cudaError_t e1 = cudaMemcpy(host.data(), s->arena, s->arena_bytes, cudaMemcpyDeviceToHost);
+  cudaError_t e2 = cudaMemcpy(dyn.data(), s->d_dyn, sizeof(CellDyn) * s->ncells, cudaMemcpyDeviceToHost);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    fclose(f);
+    return fail(s, RH_ERR_CUDA, "checkpoint copy failed");
+  }
+  int32_t hdr[4] = {1, s->opts.precision, s->ncells, 0};
+  int64_t stride = s->stride;
+  uint64_t bytes = s->arena_bytes;
+  bool ok = fwrite(kMagic, 1, 8, f) == 8 && fwrite(hdr, sizeof hdr, 1, f) == 1 &&
+            fwrite(&stride, 8, 1, f) == 1 && fwrite(&bytes, 8, 1, f) == 1 &&
+            fwrite(s->params.data(), sizeof(rh_cell_params), s->ncells, f) == (size_t)s->ncells &&
+            fwrite(host.data(), 1, host.size(), f) == host.size() &&
+            fwrite(dyn.data(), sizeof(CellDyn), s->ncells, f) == (size_t)s->ncells;
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) return fail(s, RH_ERR_IO, "write to %s failed", path);
+  return RH_OK;
+}
+
+int rh_restore(rh_sim* s, const char* path) {
+  if (!s || !path) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  FILE* f = fopen(path, "rb");
+  if (!f) return fail(s, RH_ERR_IO, "cannot open %s", path);
+  char magic[8];
+  int32_t hdr[4];
+  int64_t stride = 0;
+  uint64_t bytes = 0;
+  bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, kMagic, 8) == 0 &&
+            fread(hdr, sizeof hdr, 1, f) == 1 && fread(&stride, 8, 1, f) == 1 &&
+            fread(&bytes, 8, 1, f) == 1;
+  if (!ok || hdr[0] != 1 || hdr[1] != s->opts.precision || hdr[2] != s->ncells ||
+      stride != s->stride || bytes != s->arena_bytes) {
+    fclose(f);
+    return fail(s, RH_ERR_IO, "%s is not a snapshot of this simulator layout", path);
+  }
+  std::vector<rh_cell_params> prm(s->ncells);
+  std::vector<char> host(s->arena_bytes);
+  std::vector<CellDyn> dyn(s->ncells);
+  ok = fread(prm.data(), sizeof(rh_cell_params), s->ncells, f) == (size_t)s->ncells &&
+       fread(host.data(), 1, host.size(), f) == host.size() &&
+       fread(dyn.data(), sizeof(CellDyn), s->ncells, f) == (size_t)s->ncells;
+  fclose(f);
+  if (!ok) return fail(s, RH_ERR_IO, "%s is truncated", path);
+  if (memcmp(prm.data(), s->params.data(), sizeof(rh_cell_params) * s->ncells) != 0)
+    return fail(s, RH_ERR_IO, "%s holds different cell parameters", path);
+  CK(cudaMemcpy(s->arena, host.data(), s->arena_bytes, cudaMemcpyHostToDevice));
+  for (auto& d : dyn) d.arrive = 0;
+  CK(cudaMemcpy(s->d_dyn, dyn.data(), sizeof(CellDyn) * s->ncells, cudaMemcpyHostToDevice));
+  for (int c = 0; c < s->ncells; ++c) {
+    s->t_host[c] = dyn[c].m.t;
+    s->active_host[c] = !dyn[c].done;
+    s->drained_wc[c] = dyn[c].out_count;
+    s->drained_ls[c] = dyn[c].out_count;
+  }
+  return RH_OK;
+}
+
+int rh_state_bytes(const rh_sim* s, size_t* bytes) {
+  if (!s || !bytes) return RH_ERR_ARG;
+  *bytes = s->arena_bytes + sizeof(CellDyn) * (size_t)s->ncells;
+  return RH_OK;
+}
+
+int rh_export_state(rh_sim* s, void* host, size_t bytes) {
+  if (!s || !host || bytes != s->arena_bytes + sizeof(CellDyn) * (size_t)s->ncells)
+    return fail(s, RH_ERR_ARG, "export buffer must hold rh_state_bytes() bytes");
+  CK(cudaSetDevice(s->device));
+  char* h = reinterpret_cast<char*>(host);
+  CK(cudaMemcpyAsync(h, s->arena, s->arena_bytes, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaMemcpyAsync(h + s->arena_bytes, s->d_dyn, sizeof(CellDyn) * s->ncells,
+                     cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return RH_OK;
+}
+
+int rh_import_state(rh_sim* s, const void* host, size_t bytes) {
+  if (!s || !host || bytes != s->arena_bytes + sizeof(CellDyn) * (size_t)s->ncells)
+    return fail(s, RH_ERR_ARG, "import buffer must hold rh_state_bytes() bytes");
+  CK(cudaSetDevice(s->device));
+  const char* h = reinterpret_cast<const char*>(host);
+  const CellDyn* dyn = reinterpret_cast<const CellDyn*>(h + s->arena_bytes);
+  for (int c = 0; c < s->ncells; ++c)
+    if (dyn[c].arrive != 0) return fail(s, RH_ERR_ARG, "import block is not an exported state");
+  CK(cudaMemcpyAsync(s->arena, h, s->arena_bytes, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->d_dyn, dyn, sizeof(CellDyn) * s->ncells, cudaMemcpyHostToDevice,
+                     s->stream));
+  for (int c = 0; c < s->ncells; ++c) {
+    s->t_host[c] = dyn[c].m.t;
+    s->active_host[c] = !dyn[c].done;
+    s->drained_wc[c] = std::min(s->drained_wc[c], dyn[c].out_count);
+    s->drained_ls[c] = std::min(s->drained_ls[c], dyn[c].out_count);
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  return RH_OK;
+}
+
+int rh_bytes_per_cru_step(const rh_sim* s, double* bytes) {
+  if (!s || !bytes) return RH_ERR_ARG;
+  // 73 persistent real fields + 16 B of packed integers, each read and written once
+  *bytes = 2.0 * (73.0 * (double)real_size(s)) + 2.0 * 16.0;
+  return RH_OK;
+}
+
+int rh_kernel_timing(rh_sim* s, int64_t* launches, double* ms) {
+  if (!s || !launches || !ms) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  if (s->timing_open) {
+    CK(cudaEventSynchronize(s->ev1));
+    float e = 0;
+    CK(cudaEventElapsedTime(&e, s->ev0, s->ev1));
+    s->ms_total += e;
+    s->launches_total += s->launches_pending;
+    s->launches_pending = 0;
+    s->timing_open = false;
+  }
+  *launches = s->launches_total;
+  *ms = s->ms_total;
+  s->launches_total = 0;
+  s->ms_total = 0;
+  return RH_OK;
+}
+
+int rh_last_error(const rh_sim* s, char* buf, size_t n) {
+  if (!buf || n == 0) return RH_ERR_ARG;
+  const char* m = s ? s->err.c_str() : g_create_error.c_str();
+  snprintf(buf, n, "%s", m);
+  return RH_OK;
+}
+
+int rh_format_wholecell(const double* c, char* buf, size_t n) {
+  if (!c || !buf) return RH_ERR_ARG;
+  return snprintf(buf, n,
+                  "%f %f %f %f %f  %f %f %f %f %f  "
+                  "%f %f %f %f %f  %f %f %f %f %f  "
+                  "%f %f %f %f %f  %f %i %i %i %i  "
+                  "%i %i %i %i %i  %i %i %f %f %f  "
+                  "%i %f %f %f %f\n",
+                  c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7], c[8], c[9], c[10], c[11], c[12],
+                  c[13], c[14], c[15], c[16], c[17], c[18], c[19], c[20], c[21], c[22], c[23],
+                  c[24], c[25], (int)c[26], (int)c[27], (int)c[28], (int)c[29], (int)c[30],
+                  (int)c[31], (int)c[32], (int)c[33], (int)c[34], (int)c[35], (int)c[36], c[37],
+                  c[38], c[39], (int)c[40], c[41], c[42], c[43], c[44]);
+}
+
+int rh_format_linescan(const double* c, char* buf, size_t n) {
+  if (!c || !buf) return RH_ERR_ARG;
+  return snprintf(buf, n,
+                  "%f %f %f %i %i %i %i %i %f %f %f %f %f %f %f %f %f %f %f %f %f %f\n", c[0],
+                  c[1], c[2], (int)c[3], (int)c[4], (int)c[5], (int)c[6], (int)c[7], c[8], c[9],
+                  c[10], c[11], c[12], c[13], c[14], c[15], c[16], c[17], c[18], c[19], c[20],
+                  c[21]);
+}
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+"""Python mirror of the C ABI (include/rh.h): a batch of independent cells
+advanced on one GPU.  Every call goes through librh.so; failures raise
+NativeError with the library's error text."""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable
+
+import numpy as np
+
+from . import native
+from .abi import (LINESCAN_COLS, RH_FP64, RH_MIXED, WHOLECELL_COLS, BeatStats, CellParams,
+                  HostState, Membrane, RunOpts)
+
+PRECISIONS = {"fp64": RH_FP64, "mixed": RH_MIXED}
+
+
+def run_opts(precision: str = "fp64", **kw) -> RunOpts:
+    L = native.load()
+    o = RunOpts()
+    L.rh_default_run_opts(C.byref(o))
+    o.precision = PRECISIONS[precision]
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class Simulator:
+    def __init__(self, cells: CellParams | Iterable[CellParams], precision: str = "fp64",
+                 **opts):
+        self.L = native.load()
+        if isinstance(cells, CellParams):
+            cells = [cells]
+        cells = list(cells)
+        self.params = cells
+        self.ncells = len(cells)
+        arr = (CellParams * self.ncells)(*cells)
+        self.opts = run_opts(precision, **opts)
+        h = C.c_void_p()
+        rc = self.L.rh_create(arr, self.ncells, C.byref(self.opts), C.byref(h))
+        if rc != 0:
+            raise native.NativeError(f"rh_create failed ({rc}): {self._err(None)}")
+        self.h = h
+        self.n = []
+        for c in range(self.ncells):
+            n = C.c_int32()
+            self._ck(self.L.rh_cell_size(self.h, c, C.byref(n)))
+            self.n.append(n.value)
+
+    # -- helpers
+    def _err(self, h) -> str:
+        buf = C.create_string_buffer(1024)
+        self.L.rh_last_error(h, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def _ck(self, rc: int) -> None:
+        if rc != 0:
+            raise native.NativeError(f"librh error {rc}: {self._err(self.h)}")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.L.rh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- stepping
+    def run_steps(self, n: int) -> None:
+        self._ck(self.L.rh_run_steps(self.h, int(n)))
+
+    def run_to_end(self) -> None:
+        self._ck(self.L.rh_run_to_end(self.h))
+
+    def lattice_step(self) -> None:
+        self._ck(self.L.rh_lattice_step(self.h))
+
+    # -- state
+    def get_state(self, cell: int = 0) -> HostState:
+        hs = HostState(self.n[cell])
+        self._ck(self.L.rh_get_state(self.h, cell, C.byref(hs.view)))
+        return hs
+
+    def set_state(self, cell: int, hs: HostState) -> None:
+        self._ck(self.L.rh_set_state(self.h, cell, C.byref(hs.view)))
+
+    def get_membrane(self, cell: int = 0) -> Membrane:
+        m = Membrane()
+        self._ck(self.L.rh_get_membrane(self.h, cell, C.byref(m)))
+        return m
+
+    def set_membrane(self, cell: int, m: Membrane) -> None:
+        self._ck(self.L.rh_set_membrane(self.h, cell, C.byref(m)))
+
+    # -- outputs
+    def drain_wholecell(self, cell: int = 0, max_rec: int = 4096) -> np.ndarray:
+        a = np.zeros((max_rec, WHOLECELL_COLS))
+        n = C.c_int32()
+        self._ck(self.L.rh_drain_wholecell(self.h, cell, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                           max_rec, C.byref(n)))
+        return a[: n.value].copy()
+
+    def drain_linescan(self, cell: int = 0, max_rec: int = 4096) -> np.ndarray:
+        lx = self.params[cell].nx - 2
+        a = np.zeros((max_rec, lx, LINESCAN_COLS))
+        n = C.c_int32()
+        self._ck(self.L.rh_drain_linescan(self.h, cell, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                          max_rec, C.byref(n)))
+        return a[: n.value].copy()
+
+    def drain_stats(self, cell: int = 0, max_rec: int = 256) -> list[dict]:
+        arr = (BeatStats * max_rec)()
+        n = C.c_int32()
+        self._ck(self.L.rh_drain_stats(self.h, cell, arr, max_rec, C.byref(n)))
+        return [{k: getattr(arr[i], k) for k, _ in BeatStats._fields_ if k != "pad"}
+                for i in range(n.value)]
+
+    def status(self, cell: int = 0) -> int:
+        s = C.c_uint32()
+        self._ck(self.L.rh_cell_status(self.h, cell, C.byref(s)))
+        return s.value
+
+    def checkpoint(self, path: str) -> None:
+        self._ck(self.L.rh_checkpoint(self.h, path.encode()))
+
+    def restore(self, path: str) -> None:
+        self._ck(self.L.rh_restore(self.h, path.encode()))
+
+    def state_bytes(self) -> int:
+        b = C.c_size_t()
+        self._ck(self.L.rh_state_bytes(self.h, C.byref(b)))
+        return b.value
+
+    def export_state(self, ptr: int, nbytes: int) -> None:
+        """Copies the whole batch's state into host memory at address ptr."""
+        self._ck(self.L.rh_export_state(self.h, C.c_void_p(ptr), nbytes))
+
+    def import_state(self, ptr: int, nbytes: int) -> None:
+        self._ck(self.L.rh_import_state(self.h, C.c_void_p(ptr), nbytes))
+
+    def bytes_per_cru_step(self) -> float:
+        b = C.c_double()
+        self._ck(self.L.rh_bytes_per_cru_step(self.h, C.byref(b)))
+        return b.value
+
+    def kernel_timing(self) -> tuple[int, float]:
+        n = C.c_int64()
+        ms = C.c_double()
+        self._ck(self.L.rh_kernel_timing(self.h, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+
+def format_wholecell(row) -> str:
+    L = native.load()
+    a = np.ascontiguousarray(row, np.float64)
+    buf = C.create_string_buffer(4096)
+    L.rh_format_wholecell(a.ctypes.data_as(C.POINTER(C.c_double)), buf, 4096)
+    return buf.value.decode()
+
+
+def format_linescan(row) -> str:
+    L = native.load()
+    a = np.ascontiguousarray(row, np.float64)
+    buf = C.create_string_buffer(1024)
+    L.rh_format_linescan(a.ctypes.data_as(C.POINTER(C.c_double)), buf, 1024)
+    return buf.value.decode()

@@ -1,0 +1,86 @@
+"""Shared helpers of the GPU parity tests: building rich lattice states with
+the oracle and comparing simulator state against it."""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle import oracle as O
+from ryr_hyperactivity_gb300.abi import (DIAG_FIELDS, DIAG_SUB_FIELDS, STATE_F64_FIELDS,
+                                         STATE_INT_FIELDS, STATE_SUB_FIELDS, HostState, cell_params)
+
+COUNT_FIELDS = ["nou", "ncu", "nob", "ncb"]
+FLOAT_FIELDS = STATE_F64_FIELDS + STATE_SUB_FIELDS
+DIAG = DIAG_FIELDS + DIAG_SUB_FIELDS
+
+
+def c1_params(**kw):
+    """20x10x5 lattice (432 interior CRUs), PCL 400 ms, 2 beats."""
+    d = dict(nx=20, ny=10, nz=5, nbeats=2, pcl_ms=400.0, seed=1, cell_id=0)
+    d.update(kw)
+    return cell_params(**d)
+
+
+def rich_state(p, steps=4200, seed=0, hot_frac=0.15, to_float32=False):
+    """Oracle state after `steps` full steps (through the first beat's upstroke
+    and Ca release), with a fraction of CRUs pushed into high-cp / many-open
+    configurations so that the Gaussian RyR branches and long Poisson loops
+    run.  Returns (HostState, Membrane)."""
+    o = O.Oracle(p)
+    o.run(steps)
+    st = o.get_state()
+    m = o.get_membrane()
+    rng = np.random.default_rng(seed)
+    n = st.n
+    k = int(n * hot_frac)
+    idx = rng.choice(n, k, replace=False)
+    st["cp"][idx] = rng.uniform(15.0, 400.0, k)
+    half = idx[: k // 2]
+    nou = rng.integers(3, 45, len(half))
+    nob = rng.integers(0, 30, len(half))
+    ncb = np.minimum(st["ncb"][half], 100 - nou - nob)
+    st["nou"][half] = nou
+    st["nob"][half] = nob
+    st["ncb"][half] = ncb
+    st["ncu"][half] = 100 - nou - nob - ncb
+    if to_float32:
+        for f in FLOAT_FIELDS:
+            st[f][...] = st[f].astype(np.float32).astype(np.float64)
+    return st, m
+
+
+def rel_err(a, b, floor_frac=1e-9):
+    """max |a-b| / max(|b|, floor), floor = floor_frac * max|b| (per field)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    if a.size == 0:
+        return 0.0
+    scale = np.maximum(np.abs(b), floor_frac * max(np.max(np.abs(b)), 1e-300))
+    return float(np.max(np.abs(a - b) / scale))
+
+
+def count_mismatch(got: HostState, ref: HostState) -> np.ndarray:
+    """Boolean mask of CRUs whose RyR counts, window counters or LCC states differ."""
+    n = ref.n
+    bad = np.zeros(n, bool)
+    for f in COUNT_FIELDS + ["nl", "nspark"]:
+        bad |= got[f] != ref[f]
+    bad |= (got["lcc"] != ref["lcc"]).reshape(8, n).any(axis=0)
+    return bad
+
+
+def field_errors(got: HostState, ref: HostState, mask=None, fields=None):
+    """Per-field relative error over CRUs in `mask` (all if None)."""
+    n = ref.n
+    out = {}
+    for f in fields or (FLOAT_FIELDS + DIAG):
+        g = got[f]
+        r = ref[f]
+        if g.size == 8 * n:
+            g = g.reshape(8, n)
+            r = r.reshape(8, n)
+            if mask is not None:
+                g, r = g[:, mask], r[:, mask]
+        elif mask is not None:
+            g, r = g[mask], r[mask]
+        out[f] = rel_err(g, r)
+    return out

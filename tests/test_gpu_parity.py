@@ -1,0 +1,190 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Bars (stated in the benchmark spec): from identical state, one lattice step
+gives bit-identical RyR/LCC counts and concentrations within 1e-10 relative
+in FP64; within 1e-5 relative in the mixed (FP32 lattice) path.
+"""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from ryr_hyperactivity_gb300.abi import cell_params
+from ryr_hyperactivity_gb300.sim import Simulator
+
+from tests.gpu_helpers import (COUNT_FIELDS, DIAG, FLOAT_FIELDS, c1_params, count_mismatch,
+                          field_errors, rich_state)
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-10
+FP32_RTOL = 1e-5
+
+
+def _oracle_lattice_step(p, st, m):
+    o = O.Oracle(p)
+    o.set_state(st)
+    o.set_membrane(m)
+    o.lattice_step()
+    return o.get_state()
+
+
+def _gpu_lattice_step(p, st, m, precision):
+    with Simulator(p, precision=precision) as sim:
+        sim.set_state(0, st)
+        sim.set_membrane(0, m)
+        sim.lattice_step()
+        return sim.get_state(0)
+
+
+@pytest.mark.parametrize("variant", [dict(), dict(lqt=0, iso2=0, ku2=2.0, ikr_scale=0.3),
+                                     dict(ku=10.0, kb=1.0, tapsi=1)])
+def test_fp64_single_step_bitexact_counts(variant):
+    p = c1_params(**variant)
+    st, m = rich_state(p)
+    ref = _oracle_lattice_step(p, st, m)
+    got = _gpu_lattice_step(p, st, m, "fp64")
+    bad = count_mismatch(got, ref)
+    assert not bad.any(), f"{bad.sum()} CRUs with differing counts: {np.flatnonzero(bad)[:10]}"
+    errs = field_errors(got, ref)
+    worst = max(errs.items(), key=lambda kv: kv[1])
+    assert worst[1] <= FP64_RTOL, errs
+
+
+def test_fp64_single_step_gaussian_branches_exercised():
+    """The hot CRUs must drive the Gaussian RyR branch (pkum >= 0.2 with
+    ncu > 5): check it on the oracle's inputs, then parity."""
+    p = c1_params(ku=1.0, ku2=3.0)
+    st, m = rich_state(p, hot_frac=0.4, seed=3)
+    cp, cj, ncu = st["cp"], st["cjsr"], st["ncu"]
+    pku = 4.5 * 1.5 * 3.0 / ((1 + (5000 / cj) ** 2) * (1 + (1.0 / cp) ** 2))
+    assert np.sum((pku * 0.025 >= 0.2) & (ncu > 5)) > 10
+    ref = _oracle_lattice_step(p, st, m)
+    got = _gpu_lattice_step(p, st, m, "fp64")
+    assert not count_mismatch(got, ref).any()
+    errs = field_errors(got, ref)
+    assert max(errs.values()) <= FP64_RTOL, errs
+
+
+def test_mixed_single_step_within_fp32_tolerance():
+    p = c1_params()
+    st, m = rich_state(p, to_float32=True)
+    ref = _oracle_lattice_step(p, st, m)
+    got = _gpu_lattice_step(p, st, m, "mixed")
+    bad = count_mismatch(got, ref)
+    # float uniforms (24 bit) decide a Poisson/LCC comparison differently only
+    # when the two sides are within ~6e-8 of each other
+    assert bad.mean() <= 0.01, f"{bad.sum()} of {bad.size} CRUs differ in counts"
+    errs = field_errors(got, ref, mask=~bad)
+    assert max(errs.values()) <= FP32_RTOL, errs
+
+
+def test_fp64_full_steps_match_oracle_outputs():
+    p = c1_params()
+    nsteps = 4400  # through the first upstroke (stimulus at t = 100 ms)
+    o = O.Oracle(p)
+    _, wc_ref, ls_ref = o.run(nsteps)
+    with Simulator(p, precision="fp64") as sim:
+        sim.run_steps(nsteps)
+        wc = sim.drain_wholecell(0)
+        ls = sim.drain_linescan(0)
+        m = sim.get_membrane(0)
+        st = sim.get_state(0)
+    m_ref = o.get_membrane()
+    assert wc.shape == wc_ref.shape and ls.shape == ls_ref.shape
+    np.testing.assert_allclose(wc, wc_ref, rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(ls, ls_ref, rtol=1e-9, atol=1e-9)
+    for k in ("v", "xnai", "xm", "xh", "xj", "xr", "xs1", "qks", "xtos", "ytos", "xtof", "ytof"):
+        assert abs(getattr(m, k) - getattr(m_ref, k)) <= 1e-9 * (1 + abs(getattr(m_ref, k))), k
+    assert m.step == m_ref.step and m.t == m_ref.t
+    ref = o.get_state()
+    assert not count_mismatch(st, ref).any()
+    errs = field_errors(st, ref, fields=FLOAT_FIELDS)
+    assert max(errs.values()) <= 1e-8, errs
+
+
+def test_batched_heterogeneous_cells_match_their_oracles():
+    cells = [c1_params(nx=12, ny=9, nz=7, seed=5, cell_id=0),
+             c1_params(nx=23, ny=6, nz=4, seed=5, cell_id=1, ku2=2.5, lqt=0, iso2=0),
+             c1_params(nx=3, ny=3, nz=3, seed=9, cell_id=2),  # a single interior CRU
+             c1_params(nx=40, ny=7, nz=6, seed=5, cell_id=3, pcl_ms=300.0, cao_mM=2.2)]
+    nsteps = 4300
+    with Simulator(cells, precision="fp64") as sim:
+        sim.run_steps(nsteps)
+        for c, p in enumerate(cells):
+            o = O.Oracle(p)
+            _, wc_ref, _ = o.run(nsteps)
+            wc = sim.drain_wholecell(c)
+            np.testing.assert_allclose(wc, wc_ref, rtol=1e-9, atol=1e-9, err_msg=f"cell {c}")
+            assert not count_mismatch(sim.get_state(c), o.get_state()).any(), c
+
+
+def test_runs_are_deterministic_and_resume_bit_identically():
+    p = [c1_params(seed=3), c1_params(seed=3, cell_id=7, nx=17)]
+    with tempfile.TemporaryDirectory() as d:
+        snap = os.path.join(d, "s.bin")
+        with Simulator(p, precision="mixed") as a:
+            a.run_steps(700)
+            a.checkpoint(snap)
+            a.run_steps(650)
+            sa = [a.get_state(c).snapshot() for c in range(2)]
+            ma = [a.get_membrane(c).as_dict() for c in range(2)]
+        with Simulator(p, precision="mixed") as b:
+            b.run_steps(1350)
+            sb = [b.get_state(c).snapshot() for c in range(2)]
+        with Simulator(p, precision="mixed") as r:
+            r.restore(snap)
+            r.run_steps(650)
+            sr = [r.get_state(c).snapshot() for c in range(2)]
+            mr = [r.get_membrane(c).as_dict() for c in range(2)]
+    for c in range(2):
+        for k in sa[c]:
+            if k in DIAG:
+                continue
+            np.testing.assert_array_equal(sa[c][k], sb[c][k], err_msg=k)
+            np.testing.assert_array_equal(sa[c][k], sr[c][k], err_msg=k)
+        assert ma[c] == mr[c]
+
+
+def test_protocol_end_and_status():
+    p = c1_params(nx=6, ny=5, nz=4, nbeats=0, pcl_ms=100.0)  # runs 2100 ms
+    with Simulator(p, precision="mixed") as sim:
+        sim.run_to_end()
+        m = sim.get_membrane(0)
+        assert not (m.t < 2100.0)
+        assert sim.status(0) & 0x8
+        step = m.step
+        sim.run_steps(10)  # finished cells do not advance
+        assert sim.get_membrane(0).step == step
+        assert len(sim.drain_wholecell(0, max_rec=10000)) > 0
+
+
+def test_cli_dropin_matches_oracle_files():
+    exe = os.path.join(os.path.dirname(os.path.dirname(__file__)), "ryr_hyperactivity_gb300",
+                       "bin", "cuda_Cell_Detailed")
+    args = [1.0, 740, 1.0, 3.333, 0.00, 18.0, 0.7, 1]
+    steps = 3000
+    p = cell_params(nx=20, ny=10, nz=5, nbeats=2, pcl_ms=400.0, lqt=0, iso2=0)
+    o = O.Oracle(p)
+    _, wc_ref, ls_ref = o.run(steps)
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run([exe, "0", "x"] + [str(a) for a in args] +
+                       ["--nx", "20", "--ny", "10", "--nz", "5", "--nbeats", "2", "--pcl", "400",
+                        "--lqt", "0", "--iso2", "0", "--max-steps", str(steps)],
+                       cwd=d, check=True, capture_output=True)
+        wt = open(os.path.join(d, "wholetest_x")).read()
+        lst = open(os.path.join(d, "linescan_x")).read()
+        assert os.path.exists(os.path.join(d, "cadist_x"))
+    want_wt = O.wholecell_text(wc_ref)
+    want_ls = O.linescan_text(ls_ref)
+    a_lines, b_lines = wt.splitlines(), want_wt.splitlines()
+    assert len(a_lines) == len(b_lines)
+    for a, b in zip(a_lines, b_lines):
+        fa, fb = a.split(" "), b.split(" ")
+        assert len(fa) == len(fb)  # same fields and the same double spaces
+        va = np.array([float(x) for x in fa if x]), np.array([float(x) for x in fb if x])
+        np.testing.assert_allclose(va[0], va[1], rtol=1e-5, atol=2e-6)
+    assert len(lst.splitlines()) == len(want_ls.splitlines())
