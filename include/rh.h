@@ -54,6 +54,11 @@ extern "C" {
 #define RH_STATUS_CI_HIGH 0x4u        /* some ci > 1000 uM at an output step
                                          (cuda_Cell_Detailed.cu:878-880) */
 #define RH_STATUS_DONE 0x8u           /* the cell reached the end of its protocol */
+#define RH_STATUS_RATE_CAP 0x10u      /* an RyR transition probability per step
+                                         exceeded 1 (the OB->OU probability pbu of
+                                         subroutine_cuda.c:443 is not capped); its
+                                         Gaussian draw is then NaN, is redrawn up to
+                                         the 200-try cap and counts 0 */
 
 /* Number of columns of one wholecell record and one linescan row. */
 #define RH_WHOLECELL_COLS 45

@@ -256,6 +256,23 @@ static inline double one_minus_uniform(double u) {
   return r > 0.0 ? r : 0x1.0p-53;
 }
 
+/* Double -> int of the Gaussian draw, spelled out because C leaves NaN and
+ * out-of-range conversions undefined (x86 and aarch64 hosts disagree).  The
+ * value follows the reference's own platform: on the GB300 the conversion of
+ * NaN gives a negative integer (INT_MIN), so the draw is repeated until the
+ * 200-try cap of subroutine_cuda.c:358-361 forces 0.  NaN arises when a
+ * transition probability per step exceeds 1 (pbu, subroutine_cuda.c:443, is
+ * not capped), making n*p*(1-p) negative.  Out-of-range values saturate. */
+static inline int cuda_cvt_int(double x, uint32_t* status) {
+  if (x != x) {
+    *status |= RH_STATUS_RATE_CAP;
+    return (-2147483647 - 1);
+  }
+  if (x >= 2147483647.0) return 2147483647;
+  if (x <= -2147483648.0) return (-2147483647 - 1);
+  return (int)x;
+}
+
 /* One RyR transition count (the pattern of subroutine_cuda.c:332-363, repeated
  * for all eight transitions): Poisson by Knuth's product of uniforms, capped
  * at 195 draws, when n<=1, p<0.2 or (n<=5 and p<0.3); otherwise a Gaussian
@@ -279,9 +296,10 @@ static int ryr_transition(rh_stream* rng, int n, double p, double lam, uint32_t*
     double u1 = rh_uniform_double(rng);
     double u2 = rh_uniform_double(rng);
     unsigned int bit = rh_uniform_u32(rng);
-    m = (int)(floor(n * p + sqrt(n * p * (1.0 - p)) * sqrt(-2.0 * log(one_minus_uniform(u1))) *
-                                cos(2.0 * PI_TRUNC * u2)) +
-              bit % 2);
+    m = cuda_cvt_int(floor(n * p + sqrt(n * p * (1.0 - p)) * sqrt(-2.0 * log(one_minus_uniform(u1))) *
+                                     cos(2.0 * PI_TRUNC * u2)) +
+                         bit % 2,
+                     status);
     kk++;
     if (kk > 200) {
       m = 0;

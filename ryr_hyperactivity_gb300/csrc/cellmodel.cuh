@@ -125,19 +125,17 @@ __host__ __device__ inline void membrane_update(rh_membrane& m, double dt, doubl
   m.xitof = xitof;
 }
 
-// Voltage-only factors of the lattice update for the membrane state m.
-__host__ __device__ inline void volt_coef(VoltCoef& vc, const rh_membrane& m, const CellConst& c,
-                                          double dt) {
+// Coefficients of the next lattice update for the membrane state m.
+// Returns whether the cell is still inside its protocol (t < tend, :399).
+__host__ __device__ inline bool step_coef(StepCoef<double>& k, const rh_membrane& m,
+                                          const CellConst& c, double dt) {
   const double v = m.v, xnai = m.xnai, t = m.t;
-  vc.v = v;
-  vc.t = t;
-  vc.xnai = xnai;
   // LCC gates (reesica.h:21-63)
   double dv5 = 5, dvk = 8, fv5 = -22.8, fvk = 9.1;
-  vc.alphac = 0.22;
-  vc.betac = 4;
+  k.alphac = 0.22;
+  k.betac = 4;
   if (c.iso2) {
-    vc.betac = 2;
+    k.betac = 2;
     dv5 = 0;
     fv5 = -28;
     fvk = 8.5;
@@ -147,30 +145,42 @@ __host__ __device__ inline void volt_coef(VoltCoef& vc, const rh_membrane& m, co
   if ((v < 0.0001) && (v > -0.0001)) taudin = 0.035 * dvk / dinf;
   double finf = 1. - 1.0 / (1.0 + exp(-(v - fv5) / fvk)) / (1. + exp((v - 60) / 12.));
   double taufin = (0.02 - 0.007 * exp(-(0.0337 * (v + 10.5)) * (0.0337 * (v + 10.5))));
-  vc.alphad = dinf * taudin;
-  vc.betad = (1 - dinf) * taudin;
-  vc.alphaf = finf * taufin;
-  vc.betaf = (1 - finf) * taufin;
+  k.alphad = dinf * taudin;
+  k.betad = (1 - dinf) * taudin;
+  k.alphaf = finf * taufin;
+  k.betaf = (1 - finf) * taufin;
   // ICaL (subroutine_cuda.c:231-247)
   double za = v * FARAD / XRGAS / TEMPER;
   double e2z = exp(2.0 * za);
   if (fabs(za) < 0.001)
-    vc.lcc_k = 2.0 * PCA * FARAD * GAMMAI;
+    k.lcc_k = 2.0 * PCA * FARAD * GAMMAI;
   else
-    vc.lcc_k = 4.0 * PCA * za * FARAD * GAMMAI / (e2z - 1.0);
-  vc.lcc_e2z_k = e2z / 1000.0;
+    k.lcc_k = 4.0 * PCA * za * FARAD * GAMMAI / (e2z - 1.0);
+  k.lcc_e2z_k = e2z / 1000.0;
   // NCX (subroutine_cuda.c:56-67)
   double e1 = exp(ETA * za), e2 = exp((ETA - 1.0) * za);
   double xn3 = xnai * xnai * xnai;
   double r = xnai / KMNAI;
-  vc.ncx_num_a = e1 * xn3 * c.cao;
-  vc.ncx_num_b = e2 * (XNAO * XNAO * XNAO);
-  vc.ncx_t1 = KMCAI * (XNAO * XNAO * XNAO) * (1.0 + r * r * r);
-  vc.ncx_t3a = (KMCAO + c.cao) * xn3;
-  vc.ncx_den2 = 1.0 + KSAT * e2;
-  vc.reset_window = fmod(t - dt, OUTT) < dt;
-  vc.output_step = fmod(t + 0.0000001, OUTT) < dt;
-  vc.active = t < c.tend;
+  k.ncx_num_a = e1 * xn3 * c.cao;
+  k.ncx_num_b = e2 * (XNAO * XNAO * XNAO);
+  k.ncx_t1 = KMCAI * (XNAO * XNAO * XNAO) * (1.0 + r * r * r);
+  k.ncx_t3a = (KMCAO + c.cao) * xn3;
+  k.ncx_den2 = 1.0 + KSAT * e2;
+  k.svica = c.svica;
+  k.svncx = c.svncx;
+  k.sviup = c.sviup_tot;
+  k.cao = c.cao;
+  k.ku = c.ku;
+  k.ku2 = c.ku2;
+  k.kb = c.kb;
+  k.dt = dt;
+  k.rdt = 1.0 / dt;
+  k.dth = dt / 5.0;
+  k.rdt95 = 0.95 / dt;
+  k.rdth95 = 0.95 / (dt / 5.0);
+  k.reset_window = fmod(t - dt, OUTT) < dt;
+  k.output_step = fmod(t + 0.0000001, OUTT) < dt;
+  return t < c.tend;
 }
 
 // Output-step reductions -> the 45 wholecell columns (:931-1072).

@@ -5,8 +5,11 @@
 //     (nx-2)(ny-2)(nz-2) interior CRUs, x fastest (q = x + lx*(y + ly*z));
 //     ranges are padded to a multiple of 32 so no warp spans two cells;
 //   * per-CRU fields are one array of `stride` elements; per-sub-voxel fields
-//     are 8 planes of `stride` elements (plane ii = sub-voxel ii, bit 0 = z,
-//     bit 1 = y, bit 2 = x half, as cuda_Cell_Detailed.cu:1322-1327 defines);
+//     hold 8 values per CRU (sub-voxel ii: bit 0 = z, bit 1 = y, bit 2 = x
+//     half, as cuda_Cell_Detailed.cu:1322-1327 defines) stored as 4 planes of
+//     z-pairs: sub-voxels 2p and 2p+1 of CRU g are adjacent at
+//     (p*stride + g)*2 + {0,1} (sub_index), so one 8-byte (FP32) or 16-byte
+//     (FP64) coalesced access moves a pair;
 //   * ci, cnsr and cs are ping-ponged (two buffers, per-cell parity);
 //   * integer state packs into 16 B per CRU: RyR counts (4 x 8 bit), eight
 //     LCC slot states (8 x 8 bit) and the window counters nl (16 bit) and
@@ -23,6 +26,11 @@
 
 namespace rh {
 
+// Element index of sub-voxel ii of CRU g in a per-sub-voxel field.
+__host__ __device__ __forceinline__ int64_t sub_index(int ii, int64_t g, int64_t stride) {
+  return (((int64_t)(ii >> 1) * stride + g) << 1) | (ii & 1);
+}
+
 template <class R>
 struct Lattice {
   R* cp;
@@ -34,9 +42,9 @@ struct Lattice {
   R* casarj;
   R* casarhj;
   R* cs[2];
-  R* ci[2];    // 8 planes each
-  R* cnsr[2];  // 8 planes each
-  R* catf;     // 8 planes
+  R* ci[2];    // 4 pair planes each
+  R* cnsr[2];  // 4 pair planes each
+  R* catf;     // 4 pair planes
   R* cats;
   R* cacal;
   R* casr;
@@ -78,7 +86,8 @@ struct BeatTracker {
 // Mutable per-cell state, owned by the device between host calls.
 struct CellDyn {
   rh_membrane m;
-  VoltCoef vc;  // coefficients for the next lattice update
+  StepCoef<double> cd;  // coefficients of the next lattice update, FP64 path
+  StepCoef<float> cf;   // the same in FP32 for the mixed path
   uint32_t status;
   int parity;
   int done;
@@ -105,6 +114,17 @@ constexpr int NOUT = P_COUNT - P_STEP_END;
 // Diagnostics of the last lattice update (FP64 planes of `stride`), written
 // only when requested: xire, po, xinaca, xicat, xiup[8], xileak[8].
 enum DiagPlane { D_XIRE = 0, D_PO, D_XINACA, D_XICAT, D_XIUP, D_XILEAK = D_XIUP + 8, D_COUNT = D_XILEAK + 8 };
+
+template <class R>
+__device__ __forceinline__ const StepCoef<R>* coef_ptr(const CellDyn* d);
+template <>
+__device__ __forceinline__ const StepCoef<double>* coef_ptr<double>(const CellDyn* d) {
+  return &d->cd;
+}
+template <>
+__device__ __forceinline__ const StepCoef<float>* coef_ptr<float>(const CellDyn* d) {
+  return &d->cf;
+}
 
 template <class R>
 struct StepArgs {

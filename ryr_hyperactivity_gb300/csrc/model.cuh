@@ -6,10 +6,11 @@
 // function.  Arithmetic is arranged for sm_103a rather than copied: constant
 // divisors become reciprocal multiplies, pow(x, 23) is a product chain,
 // pow(x, 1.787) is exp(1.787 log x), and every quantity that depends only on
-// the membrane voltage is computed once per cell and step (VoltCoef), not per
+// the membrane voltage is computed once per cell and step (StepCoef), not per
 // CRU or per channel.
 #pragma once
 
+#include <limits.h>
 #include <stdint.h>
 
 #include "../../include/rh_philox.h"
@@ -94,23 +95,74 @@ struct Math<double> {
   static __device__ __forceinline__ double powpos(double x, double y) {
     return ::exp(y * ::log(x));
   }
+  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+  static __device__ __forceinline__ int to_int(double x) { return __double2int_rz(x); }
   static __device__ __forceinline__ double uniform(rh_stream* s) { return rh_uniform_double(s); }
   static constexpr double TINY_UNIFORM = 0x1.0p-53;
 };
 
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// FP32: the SFU forms (ex2/lg2/cos approximations, reciprocal division).
+// Their relative errors (~1e-6 for the arguments met here) stay well inside
+// the mixed path's 1e-5 single-step tolerance.
 template <>
 struct Math<float> {
-  static __device__ __forceinline__ float exp(float x) { return ::expf(x); }
-  static __device__ __forceinline__ float log(float x) { return ::logf(x); }
+  static __device__ __forceinline__ float exp(float x) { return __expf(x); }
+  static __device__ __forceinline__ float log(float x) { return __logf(x); }
   static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
-  static __device__ __forceinline__ float cos(float x) { return ::cosf(x); }
+  static __device__ __forceinline__ float cos(float x) { return __cosf(x); }
   static __device__ __forceinline__ float floor(float x) { return ::floorf(x); }
   static __device__ __forceinline__ float powpos(float x, float y) {
-    return ::exp2f(y * ::log2f(x));
+    return ex2_approx(y * __log2f(x));
   }
+  static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+  static __device__ __forceinline__ int to_int(float x) { return __float2int_rz(x); }
   static __device__ __forceinline__ float uniform(rh_stream* s) { return rh_uniform_float(s); }
   static constexpr float TINY_UNIFORM = 0x1.0p-24f;
 };
+
+// ---- z-pairs of sub-voxels: (lower, upper) half of a CRU in z, handled as
+//      one 2-vector.  FP32 pairs use Blackwell's packed FP32x2 instructions
+//      (add/mul/fma .f32x2); FP64 pairs are plain component-wise code. ----
+template <class R>
+struct Vec2;
+template <>
+struct Vec2<float> {
+  using T = float2;
+};
+template <>
+struct Vec2<double> {
+  using T = double2;
+};
+
+__device__ __forceinline__ float2 v2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ double2 v2(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ float2 splat2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ double2 splat2(double a) { return make_double2(a, a); }
+__device__ __forceinline__ float2 vadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 vmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 vfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a - b as fma(b, -1, a): exact product, one rounding, one packed instruction
+__device__ __forceinline__ float2 vsub(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+__device__ __forceinline__ double2 vadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 vmul(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ double2 vfma(double2 a, double2 b, double2 c) {
+  return make_double2(a.x * b.x + c.x, a.y * b.y + c.y);
+}
+__device__ __forceinline__ double2 vsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+template <class V>
+__device__ __forceinline__ V vclamp0(V a) {  // x < 0 ? 0 : x (NaN stays NaN)
+  a.x = a.x < 0 ? 0 : a.x;
+  a.y = a.y < 0 ? 0 : a.y;
+  return a;
+}
 
 template <class R>
 __device__ __forceinline__ R pow23(R x) {  // x^23 = x^16 x^4 x^2 x
@@ -146,37 +198,55 @@ __device__ __forceinline__ void csqn_mono<double>(double cjsr, double& roo2, dou
 
 template <>
 __device__ __forceinline__ void csqn_mono<float>(float cjsr, float& roo2, float& mono) {
-  roo2 = float(RATEDIMER) / (1.0f + pow23(float(KDIMER) / cjsr));
+  roo2 = __fdividef(float(RATEDIMER), 1.0f + pow23(__fdividef(float(KDIMER), cjsr)));
   float z = float(8.0 * CSQBERS) * roo2;
-  mono = (z < 0x1.0p-53f) ? 0.0f : 2.0f / (1.0f + ::sqrtf(1.0f + z));
+  mono = (z < 0x1.0p-53f) ? 0.0f : __fdividef(2.0f, 1.0f + ::sqrtf(1.0f + z));
 }
 
 // luminal buffering factor beta(cjsr) (subroutine_cuda.c:161-177)
 template <class R>
 __device__ __forceinline__ R csqn_beta(R cjsr, R roo2, R mono) {
   R ene = mono * R(NM) + (R(1) - mono) * R(ND);
-  R enedot = R(NM - ND) * (-mono + R(1) / (R(4.0 * CSQBERS) * mono * roo2 + R(1))) *
-             (R(HILLDIMER) / cjsr) * (R(1) - roo2 * R(1.0 / RATEDIMER));
+  R enedot = R(NM - ND) * (-mono + Math<R>::div(R(1), R(4.0 * CSQBERS) * mono * roo2 + R(1))) *
+             Math<R>::div(R(HILLDIMER), cjsr) * (R(1) - roo2 * R(1.0 / RATEDIMER));
   R kc = R(KBERS) + cjsr;
-  return R(1) / (R(1) + (R(CSQBERS * KBERS) * ene + R(CSQBERS) * enedot * cjsr * kc) / (kc * kc));
+  return Math<R>::div(R(1), R(1) + Math<R>::div(R(CSQBERS * KBERS) * ene +
+                                                    R(CSQBERS) * enedot * cjsr * kc,
+                                                kc * kc));
 }
 
-// ---- per-cell voltage coefficients (everything of a CRU step that depends
-//      only on v, [Na]i and the cell parameters) ----
-struct VoltCoef {
-  double v, t, xnai;
-  // LCC gates (reesica.h:37-63): d and f rates are voltage-only
-  double alphad, betad, alphaf, betaf, alphac, betac;
-  // ICaL GHK (subroutine_cuda.c:231-247): ica = lk * (cp*e2z/1000 - cao)
-  double lcc_e2z_k, lcc_k;
+// ---- per-cell coefficients of one lattice update: everything that depends
+//      only on the membrane voltage, [Na]i, time and the cell's parameters,
+//      computed once per cell and step in FP64 and stored in the kernel's
+//      precision R ----
+template <class R>
+struct StepCoef {
+  // LCC gates (reesica.h:21-63): c, d and f rates are voltage-only
+  R alphac, betac, alphad, betad, alphaf, betaf;
+  // ICaL GHK (subroutine_cuda.c:231-247): ica = lcc_k * (cpx*lcc_e2z_k - cao)
+  R lcc_e2z_k, lcc_k;
   // NCX (subroutine_cuda.c:47-75) with za and [Na]i fixed:
-  //   Inaca = Ka * (num_a - num_b cs) / ((t1 + t2(cs) + t3(cs)) den2)
-  double ncx_num_a, ncx_num_b, ncx_t1, ncx_t3a, ncx_den2;
-  int reset_window;  // fmod(t-dt, outt) < dt (:1244)
+  //   Inaca = Ka * (num_a - num_b cs) / ((t1 + t2(cs) + t3a + cs XNAO^3) den2)
+  R ncx_num_a, ncx_num_b, ncx_t1, ncx_t3a, ncx_den2;
+  // cell parameters
+  R svica, svncx, sviup, cao, ku, ku2, kb;
+  // time step constants
+  R dt, rdt, dth, rdt95, rdth95;
+  int reset_window;  // fmod(t-dt, outt) < dt (cuda_Cell_Detailed.cu:1244)
   int output_step;   // fmod(t+1e-7, outt) < dt (:777)
-  int active;
-  int pad;
 };
+
+template <class R, class Q>
+__host__ __device__ inline void convert_coef(StepCoef<R>& d, const StepCoef<Q>& s) {
+  d.alphac = R(s.alphac); d.betac = R(s.betac); d.alphad = R(s.alphad); d.betad = R(s.betad);
+  d.alphaf = R(s.alphaf); d.betaf = R(s.betaf); d.lcc_e2z_k = R(s.lcc_e2z_k); d.lcc_k = R(s.lcc_k);
+  d.ncx_num_a = R(s.ncx_num_a); d.ncx_num_b = R(s.ncx_num_b); d.ncx_t1 = R(s.ncx_t1);
+  d.ncx_t3a = R(s.ncx_t3a); d.ncx_den2 = R(s.ncx_den2); d.svica = R(s.svica); d.svncx = R(s.svncx);
+  d.sviup = R(s.sviup); d.cao = R(s.cao); d.ku = R(s.ku); d.ku2 = R(s.ku2); d.kb = R(s.kb);
+  d.dt = R(s.dt); d.rdt = R(s.rdt); d.dth = R(s.dth); d.rdt95 = R(s.rdt95); d.rdth95 = R(s.rdth95);
+  d.reset_window = s.reset_window;
+  d.output_step = s.output_step;
+}
 
 // ---- RyR transition draw (subroutine_cuda.c:332-363 and siblings) ----
 template <class R>
@@ -201,7 +271,16 @@ __device__ __forceinline__ int ryr_transition(rh_stream* rng, int n, R p, R lam,
     R om = R(1) - u1;
     if (!(om > R(0))) om = Math<R>::TINY_UNIFORM;  // u1 == 1: log(0) in the reference
     R g = sd * Math<R>::sqrt(R(-2) * Math<R>::log(om)) * Math<R>::cos(R(2.0 * PI_TRUNC) * u2);
-    m = (int)(Math<R>::floor(np + g) + R(bit % 2u));
+    R xm = Math<R>::floor(np + g) + R(bit % 2u);
+    // p > 1 makes the variance negative and the draw NaN; it converts to a
+    // negative count (as the hardware conversion does), so the draw repeats
+    // until the 200-try cap; out-of-range values saturate
+    if (xm != xm) {
+      *status |= 0x10u;  // RH_STATUS_RATE_CAP
+      m = INT_MIN;
+    } else {
+      m = Math<R>::to_int(xm);
+    }
     ++kk;
     if (kk > 200) {
       m = 0;
@@ -213,49 +292,54 @@ __device__ __forceinline__ int ryr_transition(rh_stream* rng, int n, R p, R lam,
 
 // Four-state RyR cluster step (subroutine_cuda.c:251-669).  roo2/mono come
 // from csqn_mono (the same expression the reference evaluates at :328-329).
+// The eight transitions run as one loop (their draws stay in source order);
+// each count is packed into a byte (counts are <= 195 before clamping).
 template <class R>
-__device__ __forceinline__ void ryr_gating(rh_stream* rng, R ku, R ku2, R kb, R cp, R cjsr,
-                                           R mono, R dt, int& ncu, int& nou, int& ncb, int& nob,
+__device__ __forceinline__ void ryr_gating(rh_stream* rng, const StepCoef<R>& k, R cp, R cjsr,
+                                           R mono, int& ncu, int& nou, int& ncb, int& nob,
                                            uint32_t* status) {
-  const R ryrpref = R(4.5 * 1.5);
-  R q = R(5000) / cjsr;
-  R a = ku / cp;
-  R common = R(1) / ((R(1) + q * q) * (R(1) + a * a));  // 1/(1+(5000/cjsr)^2) 1/(1+(Ku/cp)^2)
-  R pku = ryrpref * ku2 * common;
-  R pkb = R(4.5 * 1.5 / 36.) * kb * common;
+  const R dt = k.dt;
+  R q = Math<R>::div(R(5000), cjsr);
+  R a = Math<R>::div(k.ku, cp);
+  R common = Math<R>::div(R(1), (R(1) + q * q) * (R(1) + a * a));
+  R pku = R(4.5 * 1.5) * k.ku2 * common;
+  R pkb = R(4.5 * 1.5 / 36.) * k.kb * common;
   R pkuminus = R(1);  // 1/taucu
   R pkbminus = R(1);  // 1/taucb
-  if (pku * dt > R(1)) pku = R(1) / dt;
-  if (pkb * dt > R(1)) pkb = R(1) / dt;
-  if (pkuminus * dt > R(1)) pkuminus = R(1) / dt;
-  if (pkbminus * dt > R(1)) pkbminus = R(1) / dt;
+  if (pku * dt > R(1)) pku = k.rdt;
+  if (pkb * dt > R(1)) pkb = k.rdt;
+  if (pkuminus * dt > R(1)) pkuminus = k.rdt;
+  if (pkbminus * dt > R(1)) pkbminus = k.rdt;
   const R aub = mono * R(1.0 / TAUB);
   const R abu = R(1.0 / TAUU);
   const int nou0 = nou, ncu0 = ncu, nob0 = nob, ncb0 = ncb;
-
-  R pkuh = pkuminus * dt;
-  int n_ou_cu = ryr_transition<R>(rng, nou0, pkuh, Math<R>::exp(-R(nou0) * pkuh), status);
-  if (n_ou_cu > NRYR) n_ou_cu = NRYR;
-  R pkum = pku * dt;
-  int n_cu_ou = ryr_transition<R>(rng, ncu0, pkum, Math<R>::exp(-R(ncu0) * pkum), status);
-  if (n_cu_ou > NRYR) n_cu_ou = NRYR;
-  R pau = (pkb < R(1e-16)) ? R(0) : aub * dt;
-  int n_ou_ob = ryr_transition<R>(rng, nou0, pau, Math<R>::exp(-R(nou0) * pau), status);
-  if (n_ou_ob > NRYR) n_ou_ob = NRYR;
-  R pbu = (pkb < R(1e-16)) ? abu * dt * R(36) : abu * dt * (pku / pkb);
-  int n_ob_ou = ryr_transition<R>(rng, nob0, pbu, Math<R>::exp(-R(nob0) * pbu), status);
-  if (n_ob_ou > NRYR) n_ob_ou = NRYR;
-  R pcb = abu * dt;
-  int n_cb_cu = ryr_transition<R>(rng, ncb0, pcb, Math<R>::exp(-R(ncb0) * pcb), status);
-  if (n_cb_cu > NRYR) n_cb_cu = NRYR;
-  R pcub = aub * dt;
-  int n_cu_cb = ryr_transition<R>(rng, ncu0, pcub, Math<R>::exp(-R(ncu0) * pcub), status);
-  if (n_cu_cb > NRYR) n_cu_cb = NRYR;
-  R pkbh = pkbminus * dt;
-  int n_ob_cb = ryr_transition<R>(rng, nob0, pkbh, Math<R>::exp(-R(nob0) * pkbh), status);
-  R pkbm = pkb * dt;
-  int n_cb_ob = ryr_transition<R>(rng, ncb0, pkbm, Math<R>::exp(-R(ncb0) * pkbm), status);
-  if (n_cb_ob > NRYR) n_cb_ob = NRYR;
+  const R pbu = (pkb < R(1e-16)) ? abu * dt * R(36) : abu * dt * Math<R>::div(pku, pkb);
+  const R pau = (pkb < R(1e-16)) ? R(0) : aub * dt;
+  uint32_t packed0 = 0u, packed1 = 0u;
+#pragma unroll 1
+  for (int t = 0; t < 8; ++t) {
+    int n;
+    R p;
+    switch (t) {
+      case 0: n = nou0; p = pkuminus * dt; break;  // OU -> CU (:332-364)
+      case 1: n = ncu0; p = pku * dt; break;       // CU -> OU (:366-397)
+      case 2: n = nou0; p = pau; break;            // OU -> OB (:401-436)
+      case 3: n = nob0; p = pbu; break;            // OB -> OU (:439-476)
+      case 4: n = ncb0; p = abu * dt; break;       // CB -> CU (:480-511)
+      case 5: n = ncu0; p = aub * dt; break;       // CU -> CB (:513-544)
+      case 6: n = nob0; p = pkbminus * dt; break;  // OB -> CB (:548-579)
+      default: n = ncb0; p = pkb * dt; break;      // CB -> OB (:581-613)
+    }
+    int r = ryr_transition<R>(rng, n, p, Math<R>::exp(-R(n) * p), status);
+    if (t != 6) r = min(r, NRYR);  // the reference does not cap OB -> CB
+    r = min(r, 255);
+    if (t < 4) packed0 |= (uint32_t)r << (t * 8);
+    else packed1 |= (uint32_t)r << ((t - 4) * 8);
+  }
+  int n_ou_cu = packed0 & 0xff, n_cu_ou = (packed0 >> 8) & 0xff;
+  int n_ou_ob = (packed0 >> 16) & 0xff, n_ob_ou = packed0 >> 24;
+  int n_cb_cu = packed1 & 0xff, n_cu_cb = (packed1 >> 8) & 0xff;
+  int n_ob_cb = (packed1 >> 16) & 0xff, n_cb_ob = packed1 >> 24;
 
   // conflict resolution (:617-639)
   if (n_ou_ob + n_ou_cu > nou0) {

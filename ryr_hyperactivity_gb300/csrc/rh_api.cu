@@ -578,13 +578,26 @@ int get_state_t(rh_sim* s, const Lattice<R>& L, int cell, int par, rh_state_f64*
   const int n = cc.n;
   const int64_t S = s->stride;
   std::vector<R> buf(8 * (size_t)n);
+  // per-CRU fields: one plane; per-sub-voxel fields: 4 pair planes, each a
+  // contiguous run of 2n values (sub_index), de-interleaved into 8 planes
   auto pull = [&](const R* src, double* dst, int planes) -> int {
     if (!dst) return RH_OK;
-    for (int ii = 0; ii < planes; ++ii)
-      CK(cudaMemcpyAsync(buf.data() + (size_t)ii * n, src + ii * S + cc.off, sizeof(R) * n,
-                         cudaMemcpyDeviceToHost, s->stream));
+    if (planes == 1) {
+      CK(cudaMemcpyAsync(buf.data(), src + cc.off, sizeof(R) * n, cudaMemcpyDeviceToHost,
+                         s->stream));
+    } else {
+      for (int p = 0; p < 4; ++p)
+        CK(cudaMemcpyAsync(buf.data() + (size_t)p * 2 * n, src + sub_index(2 * p, cc.off, S),
+                           sizeof(R) * 2 * n, cudaMemcpyDeviceToHost, s->stream));
+    }
     CK(cudaStreamSynchronize(s->stream));
-    for (size_t q = 0; q < (size_t)n * planes; ++q) dst[q] = (double)buf[q];
+    if (planes == 1) {
+      for (size_t q = 0; q < (size_t)n; ++q) dst[q] = (double)buf[q];
+    } else {
+      for (int ii = 0; ii < 8; ++ii)
+        for (size_t q = 0; q < (size_t)n; ++q)
+          dst[(size_t)ii * n + q] = (double)buf[(size_t)(ii >> 1) * 2 * n + 2 * q + (ii & 1)];
+    }
     return RH_OK;
   };
   int r;
@@ -646,10 +659,18 @@ int set_state_t(rh_sim* s, const Lattice<R>& L, int cell, int par, const rh_stat
   std::vector<R> buf(8 * (size_t)n);
   auto push = [&](R* dst, const double* src, int planes) -> int {
     if (!src) return RH_OK;
-    for (size_t q = 0; q < (size_t)n * planes; ++q) buf[q] = (R)src[q];
-    for (int ii = 0; ii < planes; ++ii)
-      CK(cudaMemcpyAsync(dst + ii * S + cc.off, buf.data() + (size_t)ii * n, sizeof(R) * n,
-                         cudaMemcpyHostToDevice, s->stream));
+    if (planes == 1) {
+      for (size_t q = 0; q < (size_t)n; ++q) buf[q] = (R)src[q];
+      CK(cudaMemcpyAsync(dst + cc.off, buf.data(), sizeof(R) * n, cudaMemcpyHostToDevice,
+                         s->stream));
+    } else {
+      for (int ii = 0; ii < 8; ++ii)
+        for (size_t q = 0; q < (size_t)n; ++q)
+          buf[(size_t)(ii >> 1) * 2 * n + 2 * q + (ii & 1)] = (R)src[(size_t)ii * n + q];
+      for (int p = 0; p < 4; ++p)
+        CK(cudaMemcpyAsync(dst + sub_index(2 * p, cc.off, S), buf.data() + (size_t)p * 2 * n,
+                           sizeof(R) * 2 * n, cudaMemcpyHostToDevice, s->stream));
+    }
     CK(cudaStreamSynchronize(s->stream));
     return RH_OK;
   };

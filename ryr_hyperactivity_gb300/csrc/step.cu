@@ -1,18 +1,21 @@
 // step.cu — the fused per-time-step kernel.
 //
 // One launch advances every active cell by one time step:
-//   1. each CTA updates a tile of up to kBlock CRUs of one cell (the
-//      reference's Compute kernel, cuda_Cell_Detailed.cu:1187-1692, fixA),
-//      reading the previous ci/cnsr/cs buffers and writing the next ones;
+//   1. each CTA owns a tile of up to kBlock consecutive CRUs of one cell and
+//      updates them as the reference's Compute kernel does
+//      (cuda_Cell_Detailed.cu:1187-1692, fixA): the tile's own ci/cnsr
+//      sub-voxels are staged in shared memory so that in-tile stencil
+//      neighbours (+-x always, +-y when the row above/below is in the tile)
+//      come from shared memory and only the rest from L1/L2;
 //   2. the CTA reduces sum(cs), sum(xicat), sum(xinaca) (and at output steps
-//      the ~30 statistics of :839-929) with warp shuffles, compensated, and
-//      stores one partial per tile;
+//      the ~30 statistics of :839-929) with warp shuffles, error-free in the
+//      kernel's precision and compensated in FP64, and stores one partial per
+//      tile;
 //   3. the last CTA of a cell to finish (atomic arrival counter) sums the
 //      cell's partials in a fixed order, runs the membrane model and V update
 //      (:430-739, the reference's host loop), writes the output record at
-//      output steps, and prepares the voltage coefficients of the next step.
-// So the per-step device-to-host copies and host loop of the reference
-// (:427-456) disappear; a step is one kernel launch.
+//      output steps, and prepares the coefficients of the next step.
+// A time step is therefore one kernel launch with no host round trip.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -37,7 +40,7 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) 
   e = (a - (s - bb)) + (b - bb);
 }
 
-// Compensated warp sum of one value per lane; returns (sum, comp) in lane 0.
+// Compensated warp sum of one value per lane; (sum, comp) valid in lane 0.
 __device__ __forceinline__ void warp_sum_comp(double v, double& s, double& c) {
   s = v;
   c = 0.0;
@@ -81,9 +84,10 @@ __device__ __forceinline__ R clamp0(R x) {
 
 // Whole-cell part of the step, run by warp 0 of the last CTA of the cell.
 template <class R>
-__device__ void cell_update(const StepArgs<R>& a, int cell, const CellConst& cc, bool out_step) {
+__device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step) {
   const int lane = threadIdx.x & 31;
   CellDyn* dyn = a.dyn + cell;
+  const CellConst& cc = a.cells[cell];
   const double* P = a.partials;
   const int t0 = cc.tile_begin, nt = cc.tile_count;
   // fixed-order sums over the cell's tiles: lane l takes tiles l, l+32, ...
@@ -106,13 +110,14 @@ __device__ void cell_update(const StepArgs<R>& a, int cell, const CellConst& cc,
   if (out_step) {
     for (int q = 0; q < NOUT; ++q) {
       double s = 0.0;
-      for (int tl = lane; tl < nt; tl += 32) s += __ldcg(P + (size_t)(t0 + tl) * P_COUNT + P_STEP_END + q);
-      s = warp_sum(s);
-      osum[q] = s;
+      for (int tl = lane; tl < nt; tl += 32)
+        s += __ldcg(P + (size_t)(t0 + tl) * P_COUNT + P_STEP_END + q);
+      osum[q] = warp_sum(s);
     }
-    // the ci>1000 flag is a max, not a sum
+    // the ci > 1000 flag is a max, not a sum
     double f = 0.0;
-    for (int tl = lane; tl < nt; tl += 32) f = fmax(f, __ldcg(P + (size_t)(t0 + tl) * P_COUNT + O_CIHIGH));
+    for (int tl = lane; tl < nt; tl += 32)
+      f = fmax(f, __ldcg(P + (size_t)(t0 + tl) * P_COUNT + O_CIHIGH));
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) f = fmax(f, __shfl_down_sync(0xffffffffu, f, off));
     osum[O_CIHIGH - P_STEP_END] = f;
@@ -143,367 +148,423 @@ __device__ void cell_update(const StepArgs<R>& a, int cell, const CellConst& cc,
   }
   m.t = m.t + dt;  // :1083
   m.step += 1;
-  VoltCoef vc;
-  volt_coef(vc, m, cc, dt);
-  if (!vc.active) {
+  StepCoef<double> kd;
+  bool active = step_coef(kd, m, cc, dt);
+  StepCoef<float> kf;
+  convert_coef(kf, kd);
+  if (!active) {
     dyn->done = 1;
     status |= RH_STATUS_DONE;
   }
   dyn->m = m;
-  dyn->vc = vc;
+  dyn->cd = kd;
+  dyn->cf = kf;
   dyn->status = status;
 }
 
 // ------------------------------------------------------------- step kernel
 
+struct TileHeader {
+  int lx, ly, lz, nxf, nyf, tile_count, line_y, line_z;
+  uint32_t seed, cell_id;
+  long long off, ls_off, step, slot;
+  double t;
+  int parity, done;
+};
+
 template <class R, bool OUT>
-__global__ void __launch_bounds__(kBlock) step_kernel(StepArgs<R> a) {
-  __shared__ CellConst sc;
-  __shared__ VoltCoef sv;
-  __shared__ int s_parity, s_done, s_last;
-  __shared__ long long s_step, s_slot;
+__global__ void __launch_bounds__(kBlock, min_blocks<R>()) step_kernel(StepArgs<R> a) {
+  __shared__ TileHeader sh;
+  __shared__ StepCoef<R> sk;
+  using V = typename Vec2<R>::T;
+  __shared__ V s_ci2[4][kBlock];
+  __shared__ V s_cn2[4][kBlock];
   __shared__ double s_red[kBlock / 32][P_COUNT];
   __shared__ uint32_t s_status;
+  __shared__ int s_last;
 
   const int4 tile = a.tiles[blockIdx.x];
   const int cell = tile.x;
+  const int tid = threadIdx.x;
   {
-    // cooperative copy of the cell's constants and coefficients
-    const int* src = reinterpret_cast<const int*>(a.cells + cell);
-    int* dst = reinterpret_cast<int*>(&sc);
-    for (int w = threadIdx.x; w < (int)(sizeof(CellConst) / 4); w += blockDim.x) dst[w] = src[w];
-    const int* src2 = reinterpret_cast<const int*>(&a.dyn[cell].vc);
-    int* dst2 = reinterpret_cast<int*>(&sv);
-    for (int w = threadIdx.x; w < (int)(sizeof(VoltCoef) / 4); w += blockDim.x) dst2[w] = src2[w];
-    if (threadIdx.x == 0) {
-      s_parity = a.dyn[cell].parity;
-      s_done = a.dyn[cell].done;
-      s_step = a.dyn[cell].m.step;
-      s_slot = a.dyn[cell].out_count % a.out_cap;
+    const CellDyn* d = a.dyn + cell;
+    const int* src = reinterpret_cast<const int*>(coef_ptr<R>(d));
+    int* dst = reinterpret_cast<int*>(&sk);
+    for (int w = tid; w < (int)(sizeof(StepCoef<R>) / 4); w += blockDim.x) dst[w] = src[w];
+    if (tid == 0) {
+      const CellConst& c = a.cells[cell];
+      sh.lx = c.lx;
+      sh.ly = c.ly;
+      sh.lz = c.lz;
+      sh.nxf = c.nxf;
+      sh.nyf = c.nyf;
+      sh.tile_count = c.tile_count;
+      sh.line_y = c.line_y;
+      sh.line_z = c.line_z;
+      sh.seed = c.seed;
+      sh.cell_id = c.cell_id;
+      sh.off = c.off;
+      sh.ls_off = c.ls_off;
+      sh.step = d->m.step;
+      sh.t = d->m.t;
+      sh.slot = d->out_count % a.out_cap;
+      sh.parity = d->parity;
+      sh.done = d->done;
       s_status = 0;
     }
   }
   __syncthreads();
-  if (s_done) return;
+  if (sh.done) return;
 
-  const bool out_step = OUT && sv.output_step && !a.lattice_only;
+  const bool out_step = OUT && sk.output_step && !a.lattice_only;
   const Lattice<R>& L = a.L;
   const int64_t S = L.stride;
-  const int lx = sc.lx, ly = sc.ly, lz = sc.lz;
+  const int lx = sh.lx, ly = sh.ly, lz = sh.lz;
   const int lxly = lx * ly;
-  const int q = tile.y + threadIdx.x;
-  const bool valid = threadIdx.x < tile.z;
-  const int par = s_parity;
-  const R dt = R(a.dt);
-  const R dth = R(a.dt / 5.0);
+  const int count = tile.z;
+  const int q = tile.y + tid;
+  const bool valid = tid < count;
+  const int par = sh.parity;
+  const int64_t g = sh.off + q;
+  const V* ci2 = reinterpret_cast<const V*>(L.ci[par]);
+  const V* cn2 = reinterpret_cast<const V*>(L.cnsr[par]);
 
-  // per-thread partials
+  // ---- stage the tile's own sub-voxels (z-pairs) ----
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    s_ci2[p][tid] = valid ? ci2[p * S + g] : splat2(R(0));
+    s_cn2[p][tid] = valid ? cn2[p * S + g] : splat2(R(0));
+  }
+  __syncthreads();
+
   R p_cs = R(0), p_xicat = R(0), p_xinaca = R(0);
-  double o[NOUT];
+  double o[OUT ? NOUT : 1];
   if (OUT) {
 #pragma unroll
     for (int k = 0; k < NOUT; ++k) o[k] = 0.0;
   }
 
   if (valid) {
-    const int64_t g = sc.off + q;
+    const StepCoef<R>& k = sk;
+    const R dt = k.dt;
     const int x = q % lx, y = (q / lx) % ly, z = q / lxly;
-    const R* ci = L.ci[par];
-    const R* cn = L.cnsr[par];
     const R* cs = L.cs[par];
-    R* cinext = L.ci[par ^ 1];
-    R* cnnext = L.cnsr[par ^ 1];
+    V* cinext2 = reinterpret_cast<V*>(L.ci[par ^ 1]);
+    V* cnnext2 = reinterpret_cast<V*>(L.cnsr[par ^ 1]);
     R* csnext = L.cs[par ^ 1];
 
-    R cp = L.cp[g], cjsr = L.cjsr[g], cjsrb = L.cjsrb[g], ancx = L.ancx[g];
+    R cp = L.cp[g], cjsr = L.cjsr[g];
     const R cs0 = cs[g];
-    uint32_t ryr = L.ryr[g];
+    // ---- dyad/submembrane/JSR coupling terms from the old state (:1309-1314) ----
+    const R ci0 = s_ci2[0][tid].x, ci1 = s_ci2[0][tid].y;
+    const R cn0 = s_cn2[0][tid].x, cn1 = s_cn2[0][tid].y;
+    const R diffpi0 = (cp - ci0) * R(1.0 / TAUPI / 2.);
+    const R diffpi1 = (cp - ci1) * R(1.0 / TAUPI / 2.);
+    const R diffsi0 = (cs0 - ci0) * R(1.0 / TAUSI / 2.);
+    const R diffsi1 = (cs0 - ci1) * R(1.0 / TAUSI / 2.);
+    const R diffjn0 = (cjsr - cn0) * R(1.0 / TAUTR / 2.);
+    const R diffjn1 = (cjsr - cn1) * R(1.0 / TAUTR / 2.);
+
+    // ---- sub-voxel diffusion, SERCA/leak, cytosolic buffers (:1305-1393) ----
+    // Processed as four z-pairs p = (sub-voxels 2p, 2p+1).  Along z the pair's
+    // halves are each other's neighbour; the outer neighbours are the
+    // adjacent CRUs' pair p.  Along y (x) the neighbour pair is p^1 (p^2) of
+    // this CRU or of the adjacent CRU in the direction of the pair's y (x)
+    // bit.  At a lattice face the zero-flux ghost equals the sub-voxel
+    // itself (:1601-1652), so that difference vanishes.
+    const bool has_zp = z + 1 < lz, has_zm = z > 0;
+    const bool has_yp = y + 1 < ly, has_ym = y > 0;
+    const bool has_xp = x + 1 < lx, has_xm = x > 0;
+    const bool zp_in = tid + lxly < count, zm_in = tid - lxly >= 0;
+    const bool yp_in = tid + lx < count, ym_in = tid - lx >= 0;
+    const bool xp_in = tid + 1 < count, xm_in = tid - 1 >= 0;
+    const V kt_n = splat2(R(1.0 / (TAUNT * XI))), kl_n = splat2(R(1.0 / (TAUNL * XI)));
+    const V kt_i = splat2(R(1.0 / (TAUIT * XI))), kl_i = splat2(R(1.0 / (TAUIL * XI)));
+    const V dt2 = splat2(dt);
+    const V* catf2 = reinterpret_cast<const V*>(L.catf);
+    const V* cats2 = reinterpret_cast<const V*>(L.cats);
+    const V* cacal2 = reinterpret_cast<const V*>(L.cacal);
+    const V* casr2 = reinterpret_cast<const V*>(L.casr);
+    const V* camyo2 = reinterpret_cast<const V*>(L.camyo);
+    const V* mgmyo2 = reinterpret_cast<const V*>(L.mgmyo);
+    V* catf2w = reinterpret_cast<V*>(L.catf);
+    V* cats2w = reinterpret_cast<V*>(L.cats);
+    V* cacal2w = reinterpret_cast<V*>(L.cacal);
+    V* casr2w = reinterpret_cast<V*>(L.casr);
+    V* camyo2w = reinterpret_cast<V*>(L.camyo);
+    V* mgmyo2w = reinterpret_cast<V*>(L.mgmyo);
+    R sum_ci = R(0), sum_cn = R(0), sum_catf = R(0), sum_cats = R(0), sum_casr = R(0);
+    R sum_camyo = R(0), sum_cacal = R(0), sum_up = R(0), sum_lk = R(0);
+    bool ci_high = false;
+#pragma unroll 1
+    for (int p = 0; p < 4; ++p) {
+      const int by = p & 1, bx = p >> 1;
+      const int64_t gp = p * S + g;
+      const V c = s_ci2[p][tid], n = s_cn2[p][tid];
+      // z
+      V czp = c, nzp = n, czm = c, nzm = n;
+      if (has_zp) {
+        if (zp_in) {
+          czp = s_ci2[p][tid + lxly];
+          nzp = s_cn2[p][tid + lxly];
+        } else {
+          czp = __ldg(ci2 + gp + lxly);
+          nzp = __ldg(cn2 + gp + lxly);
+        }
+      }
+      if (has_zm) {
+        if (zm_in) {
+          czm = s_ci2[p][tid - lxly];
+          nzm = s_cn2[p][tid - lxly];
+        } else {
+          czm = __ldg(ci2 + gp - lxly);
+          nzm = __ldg(cn2 + gp - lxly);
+        }
+      }
+      const V ciN = v2(c.y, has_zp ? czp.x : c.y), cnN = v2(n.y, has_zp ? nzp.x : n.y);
+      const V ciS = v2(has_zm ? czm.y : c.x, c.x), cnS = v2(has_zm ? nzm.y : n.x, n.x);
+      // y: pair p^1
+      V ciE, cnE, ciW, cnW;
+      {
+        const int py = p ^ 1;
+        const V ci_in = s_ci2[py][tid], cn_in = s_cn2[py][tid];
+        V ci_ex = c, cn_ex = n;
+        const int d = by ? lx : -lx;
+        if (by ? has_yp : has_ym) {
+          if (by ? yp_in : ym_in) {
+            ci_ex = s_ci2[py][tid + d];
+            cn_ex = s_cn2[py][tid + d];
+          } else {
+            ci_ex = __ldg(ci2 + py * S + g + d);
+            cn_ex = __ldg(cn2 + py * S + g + d);
+          }
+        }
+        ciE = by ? ci_ex : ci_in;
+        cnE = by ? cn_ex : cn_in;
+        ciW = by ? ci_in : ci_ex;
+        cnW = by ? cn_in : cn_ex;
+      }
+      // x: pair p^2
+      V ciT, cnT, ciB, cnB;
+      {
+        const int px = p ^ 2;
+        const V ci_in = s_ci2[px][tid], cn_in = s_cn2[px][tid];
+        V ci_ex = c, cn_ex = n;
+        const int d = bx ? 1 : -1;
+        if (bx ? has_xp : has_xm) {
+          if (bx ? xp_in : xm_in) {
+            ci_ex = s_ci2[px][tid + d];
+            cn_ex = s_cn2[px][tid + d];
+          } else {
+            ci_ex = __ldg(ci2 + px * S + g + d);
+            cn_ex = __ldg(cn2 + px * S + g + d);
+          }
+        }
+        ciT = bx ? ci_ex : ci_in;
+        cnT = bx ? cn_ex : cn_in;
+        ciB = bx ? ci_in : ci_ex;
+        cnB = bx ? cn_in : cn_ex;
+      }
+      const V coupn = vfma(vadd(vadd(vadd(vsub(cnN, n), vsub(cnS, n)), vsub(cnE, n)), vsub(cnW, n)),
+                           kt_n, vmul(vadd(vsub(cnT, n), vsub(cnB, n)), kl_n));
+      const V coupi = vfma(vadd(vadd(vadd(vsub(ciN, c), vsub(ciS, c)), vsub(ciE, c)), vsub(ciW, c)),
+                           kt_i, vmul(vadd(vsub(ciT, c), vsub(ciB, c)), kl_i));
+      // SERCA and leak (subroutine_cuda.c:128-146)
+      V up, lk;
+      {
+        const R pax = Math<R>::powpos(c.x * R(1.0 / KI_UP), R(HH_UP));
+        const R pay = Math<R>::powpos(c.y * R(1.0 / KI_UP), R(HH_UP));
+        const R pbx = Math<R>::powpos(n.x * R(1.0 / KNSR_UP), R(HH_UP));
+        const R pby = Math<R>::powpos(n.y * R(1.0 / KNSR_UP), R(HH_UP));
+        up = v2(k.sviup * Math<R>::div(R(VUP) * (pax - pbx), R(1) + pax + pbx),
+                k.sviup * Math<R>::div(R(VUP) * (pay - pby), R(1) + pay + pby));
+        const V n2 = vmul(n, n);
+        const V num = vmul(vmul(splat2(R(GLEAK)), vsub(n, c)), n2);
+        const V den = vadd(n2, splat2(R(KJSR_LEAK * KJSR_LEAK)));
+        lk = v2(Math<R>::div(num.x, den.x), Math<R>::div(num.y, den.y));
+      }
+      // cytosolic buffers (buffers.c:55-115): on*(B-b) - koff*b, with the
+      // saturation guard kon*c*dt > 1 taken on the rare slow path
+      V catf = catf2[gp], cats = cats2[gp], cacal = cacal2[gp], casr = casr2[gp];
+      V camyo = camyo2[gp], mgmyo = mgmyo2[gp];
+      const V freemyo = vsub(vsub(splat2(R(BMYO)), camyo), mgmyo);
+      V r_tf = vfma(vmul(splat2(R(KTFON)), c), vsub(splat2(R(BTF)), catf), vmul(splat2(R(-KTFOFF)), catf));
+      V r_ts = vfma(vmul(splat2(R(KTSON)), c), vsub(splat2(R(BTS)), cats), vmul(splat2(R(-KTSOFF)), cats));
+      V r_cal = vfma(vmul(splat2(R(KCALON)), c), vsub(splat2(R(BCAL)), cacal),
+                     vmul(splat2(R(-KCALOFF)), cacal));
+      V r_sr = vfma(vmul(splat2(R(KSRON)), c), vsub(splat2(R(BSR)), casr), vmul(splat2(R(-KSROFF)), casr));
+      V r_mc = vfma(vmul(splat2(R(KONMYOCA)), c), freemyo, vmul(splat2(R(-KOFFMYOCA)), camyo));
+      if (fmax(c.x, c.y) * R(KONMYOCA) * dt > R(1)) {  // some buffer saturates
+        const R cc[2] = {c.x, c.y};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const R cv = cc[h];
+          R& tf = h ? r_tf.y : r_tf.x;
+          R& ts = h ? r_ts.y : r_ts.x;
+          R& cal = h ? r_cal.y : r_cal.x;
+          R& sr = h ? r_sr.y : r_sr.x;
+          R& mc = h ? r_mc.y : r_mc.x;
+          tf = buffer_rate<R>(R(KTFON), R(KTFOFF), R(BTF), h ? catf.y : catf.x, cv, dt, k.rdt95);
+          ts = buffer_rate<R>(R(KTSON), R(KTSOFF), R(BTS), h ? cats.y : cats.x, cv, dt, k.rdt95);
+          cal = buffer_rate<R>(R(KCALON), R(KCALOFF), R(BCAL), h ? cacal.y : cacal.x, cv, dt, k.rdt95);
+          sr = buffer_rate<R>(R(KSRON), R(KSROFF), R(BSR), h ? casr.y : casr.x, cv, dt, k.rdt95);
+          const R fmy = h ? freemyo.y : freemyo.x;
+          const R cm = h ? camyo.y : camyo.x;
+          const R onmc = R(KONMYOCA) * cv;
+          mc = (onmc * dt > R(1)) ? k.rdt95 * fmy - R(KOFFMYOCA) * cm : onmc * fmy - R(KOFFMYOCA) * cm;
+        }
+      }
+      V dotcn = vfma(vsub(up, lk), splat2(R(VI / VNSR)), coupn);
+      V dotci = vadd(vsub(vsub(lk, up), vadd(vadd(vadd(vadd(r_tf, r_ts), r_cal), r_sr), r_mc)), coupi);
+      if (p == 0) {  // sub-voxels 0 and 1 touch the dyad, submembrane and JSR (:1356-1361)
+        dotcn = vfma(v2(diffjn0, diffjn1), splat2(R(VJSR / VNSR)), dotcn);
+        dotci = vfma(v2(diffsi0, diffsi1), splat2(R(VS / VI)), dotci);
+        dotci = vfma(v2(diffpi0, diffpi1), splat2(R(VP / VI)), dotci);
+      }
+      const V cinew = vclamp0(vfma(dotci, dt2, c));
+      const V cnnew = vfma(dotcn, dt2, n);
+      catf = vclamp0(vfma(r_tf, dt2, catf));
+      cats = vclamp0(vfma(r_ts, dt2, cats));
+      cacal = vclamp0(vfma(r_cal, dt2, cacal));
+      casr = vclamp0(vfma(r_sr, dt2, casr));
+      camyo = vclamp0(vfma(r_mc, dt2, camyo));
+      {
+        const V fm = vsub(vsub(splat2(R(BMYO)), camyo), mgmyo);
+        V r_mg = vfma(splat2(R(KONMYOMG * MGI)), fm, vmul(splat2(R(-KOFFMYOMG)), mgmyo));
+        if (R(KONMYOMG * MGI) * dt > R(1)) {  // guard of myomg (buffers.c:65)
+          r_mg = vfma(splat2(k.rdt95), fm, vmul(splat2(R(-KOFFMYOMG)), mgmyo));
+        }
+        mgmyo = vclamp0(vfma(r_mg, dt2, mgmyo));
+      }
+      cinext2[gp] = cinew;
+      cnnext2[gp] = cnnew;
+      catf2w[gp] = catf;
+      cats2w[gp] = cats;
+      cacal2w[gp] = cacal;
+      casr2w[gp] = casr;
+      camyo2w[gp] = camyo;
+      mgmyo2w[gp] = mgmyo;
+      if (a.diag) {
+        a.diag[(int64_t)(D_XIUP + 2 * p) * S + g] = (double)up.x;
+        a.diag[(int64_t)(D_XIUP + 2 * p + 1) * S + g] = (double)up.y;
+        a.diag[(int64_t)(D_XILEAK + 2 * p) * S + g] = (double)lk.x;
+        a.diag[(int64_t)(D_XILEAK + 2 * p + 1) * S + g] = (double)lk.y;
+      }
+      if (OUT && out_step) {
+        sum_ci += cinew.x + cinew.y;
+        sum_cn += cnnew.x + cnnew.y;
+        sum_catf += catf.x + catf.y;
+        sum_cats += cats.x + cats.y;
+        sum_casr += casr.x + casr.y;
+        sum_camyo += camyo.x + camyo.y;
+        sum_cacal += cacal.x + cacal.y;
+        sum_up += up.x + up.y;
+        sum_lk += lk.x + lk.y;
+        ci_high |= (cinew.x > R(1000)) || (cinew.y > R(1000));
+      }
+    }
+
+    // ---- CRU state of the stochastic part ----
+    R cjsrb = L.cjsrb[g], ancx = L.ancx[g];
+    const uint32_t ryr = L.ryr[g];
     uint2 lccw = L.lcc[g];
-    uint32_t win = L.win[g];
+    const uint32_t win = L.win[g];
     int nou = ryr & 0xff, ncu = (ryr >> 8) & 0xff, nob = (ryr >> 16) & 0xff, ncb = ryr >> 24;
     int nl = win & 0xffff, nspark = win >> 16;
-    if (sv.reset_window) {  // :1244-1247
+    if (k.reset_window) {  // :1244-1247
       nl = 0;
       nspark = 0;
     }
     uint32_t status = 0;
     rh_stream rng;
-    const uint32_t pos = (uint32_t)((x + 1) + sc.nxf * ((y + 1) + sc.nyf * (z + 1)));
-    rh_stream_init(&rng, sc.seed, sc.cell_id, pos, (uint64_t)s_step);
+    const uint32_t pos = (uint32_t)((x + 1) + sh.nxf * ((y + 1) + sh.nyf * (z + 1)));
+    rh_stream_init(&rng, sh.seed, sh.cell_id, pos, (uint64_t)sh.step);
 
     // ---- LCC channels (:1248-1263, reesica.h:14-116) ----
-    const R cpx = (cp + cs0 * R(ICAGAMMA)) / R(1 + ICAGAMMA);
-    const R rdt = R(1.0 / a.dt);
+    const R cpx = Math<R>::div(cp + cs0 * R(ICAGAMMA), R(1 + ICAGAMMA));
     R bfca;
     {
-      R qq = R(25) / cpx;
-      bfca = R(0.175) / (R(1) + qq * qq);
+      R qq = Math<R>::div(R(25), cpx);
+      bfca = Math<R>::div(R(0.175), R(1) + qq * qq);
     }
     int nlcp = 0;
     {
-      const R ac = R(sv.alphac), bc = R(sv.betac), ad = R(sv.alphad), bd = R(sv.betad);
-      const R af = R(sv.alphaf), bf = R(sv.betaf), afca = R(0.012 / 2.);
-      uint32_t w0 = lccw.x, w1 = lccw.y;
-      bool stop = false;
-#pragma unroll
+      uint64_t slots = ((uint64_t)lccw.y << 32) | lccw.x;
+#pragma unroll 1
       for (int ll = 0; ll < 8; ++ll) {
-        uint32_t& wd = (ll < 4) ? w0 : w1;
-        const int sh = (ll & 3) * 8;
-        int st = (wd >> sh) & 0xff;
-        if (!stop && st < 16) {
-          R u = Math<R>::uniform(&rng);
-          st = lcc_next<R>(st, u * rdt, ac, bc, ad, bd, af, bf, afca, bfca);
-          wd = (wd & ~(0xffu << sh)) | ((uint32_t)st << sh);
-          if (st == 0) {
-            ++nl;
-            ++nlcp;
-          }
-        } else {
-          stop = true;
+        const int sh8 = ll * 8;
+        int st = (int)((slots >> sh8) & 0xff);
+        if (st >= 16) break;  // the reference stops at the first empty slot
+        R u = Math<R>::uniform(&rng);
+        st = lcc_next<R>(st, u * k.rdt, k.alphac, k.betac, k.alphad, k.betad, k.alphaf, k.betaf,
+                         R(0.012 / 2.), bfca);
+        slots = (slots & ~(0xffull << sh8)) | ((uint64_t)st << sh8);
+        if (st == 0) {
+          ++nl;
+          ++nlcp;
         }
       }
-      lccw.x = w0;
-      lccw.y = w1;
+      lccw.x = (uint32_t)slots;
+      lccw.y = (uint32_t)(slots >> 32);
     }
     R icat1;
     {
-      R ica = R(sv.lcc_k) * (cpx * R(sv.lcc_e2z_k) - R(sc.cao));
+      R ica = k.lcc_k * (cpx * k.lcc_e2z_k - k.cao);
       if (ica > R(0)) ica = R(0);
-      icat1 = R(sc.svica) * R(nlcp) * ica;
+      icat1 = k.svica * R(nlcp) * ica;
     }
 
     // ---- RyR gating, spark flag, release (:1274-1293) ----
     R roo2, mono;
     csqn_mono<R>(cjsr, roo2, mono);
     const int prevsp = nou + nob;
-    ryr_gating<R>(&rng, R(sc.ku), R(sc.ku2), R(sc.kb), cp, cjsr, mono, dt, ncu, nou, ncb, nob,
-                  &status);
+    ryr_gating<R>(&rng, k, cp, cjsr, mono, ncu, nou, ncb, nob, &status);
     if (prevsp < 5 && nou + nob >= 5) nspark = 1;
-    const R po = R(nou + nob) / R(NRYR);
+    const R po = Math<R>::div(R(nou + nob), R(NRYR));
     R xire = R(0.0147 * SVJMAX) * po * (cjsr - cp) * R(1.0 / VP);
     if (xire < R(0)) xire = R(0);
 
     // ---- NCX (:1296, subroutine_cuda.c:47-75) ----
     R xinaca;
     {
-      const R csm = cs0 / R(1000);
+      const R csm = cs0 * R(1e-3);
       const R t2 = R(KMNAO * KMNAO * KMNAO) * csm * (R(1) + csm * R(1.0 / KMCAI));
-      const R t3 = R(sv.ncx_t3a) + csm * R(XNAO * XNAO * XNAO);
-      const R inaca = ancx * R(VNACA) * (R(sv.ncx_num_a) - R(sv.ncx_num_b) * csm) /
-                      ((R(sv.ncx_t1) + t2 + t3) * R(sv.ncx_den2));
-      const R r3 = R(0.0003) / csm;
-      ancx += (R(1) / (R(1) + r3 * r3 * r3) - ancx) * R(1.0 / 150.) * dt;
-      xinaca = R(sc.svncx) * inaca;
+      const R t3 = k.ncx_t3a + csm * R(XNAO * XNAO * XNAO);
+      const R inaca = Math<R>::div(ancx * R(VNACA) * (k.ncx_num_a - k.ncx_num_b * csm),
+                                   (k.ncx_t1 + t2 + t3) * k.ncx_den2);
+      const R r3 = Math<R>::div(R(0.0003), csm);
+      ancx += (Math<R>::div(R(1), R(1) + r3 * r3 * r3) - ancx) * R(1.0 / 150.) * dt;
+      xinaca = k.svncx * inaca;
     }
 
-    // ---- own sub-voxels (old values) ----
-    R cio[8], cno[8];
-#pragma unroll
-    for (int ii = 0; ii < 8; ++ii) {
-      cio[ii] = ci[ii * S + g];
-      cno[ii] = cn[ii * S + g];
-    }
-
-    // ---- dyad/submembrane/JSR couplings and CSQN (:1309-1317) ----
-    const R diffpi0 = (cp - cio[0]) * R(1.0 / TAUPI / 2.);
-    const R diffpi1 = (cp - cio[1]) * R(1.0 / TAUPI / 2.);
-    const R diffsi0 = (cs0 - cio[0]) * R(1.0 / TAUSI / 2.);
-    const R diffsi1 = (cs0 - cio[1]) * R(1.0 / TAUSI / 2.);
-    const R diffjn0 = (cjsr - cno[0]) * R(1.0 / TAUTR / 2.);
-    const R diffjn1 = (cjsr - cno[1]) * R(1.0 / TAUTR / 2.);
+    // ---- CSQN buffering of the JSR (:1316-1317) ----
     const R beta = csqn_beta<R>(cjsr, roo2, mono);
     const R jterm = (-diffjn0 - diffjn1) - xire * R(VP / VJSR);
     const R dotcjsr = beta * jterm;
     cjsrb += (R(1) - beta) * jterm * dt;
 
-    // ---- sub-voxel diffusion, SERCA/leak, cytosolic buffers (:1305-1393) ----
-    const bool has_zp = z + 1 < lz, has_zm = z > 0;
-    const bool has_yp = y + 1 < ly, has_ym = y > 0;
-    const bool has_xp = x + 1 < lx, has_xm = x > 0;
-    const R kt_n = R(1.0 / (TAUNT * XI)), kl_n = R(1.0 / (TAUNL * XI));
-    const R kt_i = R(1.0 / (TAUIT * XI)), kl_i = R(1.0 / (TAUIL * XI));
-    const R sviup = R(sc.sviup_tot);
-    const R rdt95 = R(0.95 / a.dt);
-    R sum_ci = R(0), sum_cn = R(0), sum_catf = R(0), sum_cats = R(0), sum_casr = R(0);
-    R sum_camyo = R(0), sum_cacal = R(0), sum_up = R(0), sum_lk = R(0);
-    R ci_sub0 = R(0), camyo0 = R(0), mgmyo0 = R(0), casr0 = R(0), cacal0 = R(0), cats0 = R(0),
-      catf0 = R(0);
-    bool ci_high = false;
-#pragma unroll
-    for (int ii = 0; ii < 8; ++ii) {
-      const int bz = ii & 1, by = (ii >> 1) & 1, bx = (ii >> 2) & 1;
-      const R c = cio[ii], n = cno[ii];
-      // +z / -z
-      R ciN, cnN, ciS, cnS;
-      if (bz) {
-        ciS = cio[ii - 1];
-        cnS = cno[ii - 1];
-        if (has_zp) {
-          ciN = __ldg(ci + (ii - 1) * S + g + lxly);
-          cnN = __ldg(cn + (ii - 1) * S + g + lxly);
-        } else {
-          ciN = c;
-          cnN = n;
-        }
-      } else {
-        ciN = cio[ii + 1];
-        cnN = cno[ii + 1];
-        if (has_zm) {
-          ciS = __ldg(ci + (ii + 1) * S + g - lxly);
-          cnS = __ldg(cn + (ii + 1) * S + g - lxly);
-        } else {
-          ciS = c;
-          cnS = n;
-        }
-      }
-      // +y / -y
-      R ciE, cnE, ciW, cnW;
-      if (by) {
-        ciW = cio[ii - 2];
-        cnW = cno[ii - 2];
-        if (has_yp) {
-          ciE = __ldg(ci + (ii - 2) * S + g + lx);
-          cnE = __ldg(cn + (ii - 2) * S + g + lx);
-        } else {
-          ciE = c;
-          cnE = n;
-        }
-      } else {
-        ciE = cio[ii + 2];
-        cnE = cno[ii + 2];
-        if (has_ym) {
-          ciW = __ldg(ci + (ii + 2) * S + g - lx);
-          cnW = __ldg(cn + (ii + 2) * S + g - lx);
-        } else {
-          ciW = c;
-          cnW = n;
-        }
-      }
-      // +x / -x
-      R ciT, cnT, ciB, cnB;
-      if (bx) {
-        ciB = cio[ii - 4];
-        cnB = cno[ii - 4];
-        if (has_xp) {
-          ciT = __ldg(ci + (ii - 4) * S + g + 1);
-          cnT = __ldg(cn + (ii - 4) * S + g + 1);
-        } else {
-          ciT = c;
-          cnT = n;
-        }
-      } else {
-        ciT = cio[ii + 4];
-        cnT = cno[ii + 4];
-        if (has_xm) {
-          ciB = __ldg(ci + (ii + 4) * S + g - 1);
-          cnB = __ldg(cn + (ii + 4) * S + g - 1);
-        } else {
-          ciB = c;
-          cnB = n;
-        }
-      }
-      const R coupn = ((cnN - n) + (cnS - n) + (cnE - n) + (cnW - n)) * kt_n +
-                      ((cnT - n) + (cnB - n)) * kl_n;
-      const R coupi = ((ciN - c) + (ciS - c) + (ciE - c) + (ciW - c)) * kt_i +
-                      ((ciT - c) + (ciB - c)) * kl_i;
-      // SERCA and leak (subroutine_cuda.c:128-146)
-      const R pa = Math<R>::powpos(c * R(1.0 / KI_UP), R(HH_UP));
-      const R pb = Math<R>::powpos(n * R(1.0 / KNSR_UP), R(HH_UP));
-      const R up = sviup * (R(VUP) * (pa - pb) / (R(1) + pa + pb));
-      const R n2 = n * n;
-      const R lk = R(GLEAK) * (n - c) * n2 / (n2 + R(KJSR_LEAK * KJSR_LEAK));
-      // buffers (buffers.c:55-115)
-      const int64_t gi = ii * S + g;
-      R catf = L.catf[gi], cats = L.cats[gi], cacal = L.cacal[gi], casr = L.casr[gi];
-      R camyo = L.camyo[gi], mgmyo = L.mgmyo[gi];
-      const R r_tf = buffer_rate<R>(R(KTFON), R(KTFOFF), R(BTF), catf, c, dt, rdt95);
-      const R r_ts = buffer_rate<R>(R(KTSON), R(KTSOFF), R(BTS), cats, c, dt, rdt95);
-      const R r_cal = buffer_rate<R>(R(KCALON), R(KCALOFF), R(BCAL), cacal, c, dt, rdt95);
-      const R r_sr = buffer_rate<R>(R(KSRON), R(KSROFF), R(BSR), casr, c, dt, rdt95);
-      const R freemyo = R(BMYO) - camyo - mgmyo;
-      const R onmc = R(KONMYOCA) * c;
-      const R r_mc = (onmc * dt > R(1)) ? rdt95 * freemyo - R(KOFFMYOCA) * camyo
-                                        : onmc * freemyo - R(KOFFMYOCA) * camyo;
-      R dotcn = (up - lk) * R(VI / VNSR) + coupn;
-      R dotci = (-up + lk) - (r_tf + r_ts + r_cal + r_sr + r_mc) + coupi;
-      if (ii == 0) {
-        dotcn += diffjn0 * R(VJSR / VNSR);
-        dotci += diffsi0 * R(VS / VI);
-        dotci += diffpi0 * R(VP / VI);
-      } else if (ii == 1) {
-        dotcn += diffjn1 * R(VJSR / VNSR);
-        dotci += diffsi1 * R(VS / VI);
-        dotci += diffpi1 * R(VP / VI);
-      }
-      const R cinew = clamp0(c + dotci * dt);
-      const R cnnew = n + dotcn * dt;
-      catf = clamp0(catf + r_tf * dt);
-      cats = clamp0(cats + r_ts * dt);
-      cacal = clamp0(cacal + r_cal * dt);
-      casr = clamp0(casr + r_sr * dt);
-      camyo = clamp0(camyo + r_mc * dt);
-      {
-        const R fm = R(BMYO) - camyo - mgmyo;
-        const R onmg = R(KONMYOMG * MGI);
-        const R r_mg = (onmg * dt > R(1)) ? rdt95 * fm - R(KOFFMYOMG) * mgmyo
-                                          : onmg * fm - R(KOFFMYOMG) * mgmyo;
-        mgmyo = clamp0(mgmyo + r_mg * dt);
-      }
-      cinext[gi] = cinew;
-      cnnext[gi] = cnnew;
-      L.catf[gi] = catf;
-      L.cats[gi] = cats;
-      L.cacal[gi] = cacal;
-      L.casr[gi] = casr;
-      L.camyo[gi] = camyo;
-      L.mgmyo[gi] = mgmyo;
-      if (a.diag) {
-        a.diag[(int64_t)(D_XIUP + ii) * S + g] = (double)up;
-        a.diag[(int64_t)(D_XILEAK + ii) * S + g] = (double)lk;
-      }
-      if (out_step) {
-        sum_ci += cinew;
-        sum_cn += cnnew;
-        sum_catf += catf;
-        sum_cats += cats;
-        sum_casr += casr;
-        sum_camyo += camyo;
-        sum_cacal += cacal;
-        sum_up += up;
-        sum_lk += lk;
-        ci_high |= cinew > R(1000);
-        if (ii == 0) {
-          ci_sub0 = cinew;
-          camyo0 = camyo;
-          mgmyo0 = mgmyo;
-          casr0 = casr;
-          cacal0 = cacal;
-          cats0 = cats;
-          catf0 = catf;
-        }
-      }
-    }
-
     // ---- five sub-steps of cs, cp and the sarcolemmal buffers (:1396-1473) ----
     R casar = L.casar[g], casarh = L.casarh[g], casarj = L.casarj[g], casarhj = L.casarhj[g];
     R csn = cs0;
     {
+      const R dth = k.dth, rdth95 = k.rdth95;
       const R csN = has_zp ? __ldg(cs + g + lxly) : cs0;
       const R csS = has_zm ? __ldg(cs + g - lxly) : cs0;
       const R csdiff = (csN + csS - R(2) * cs0) * R(1.0 / TAUST);
       const R cs_const = -R(ICAGAMMA * VP / VS) * icat1 + xinaca -
-                         (cs0 - cio[0]) * R(1.0 / TAUSI / 2.) -
-                         (cs0 - cio[1]) * R(1.0 / TAUSI / 2.) + csdiff;
-      const R cp_const = (cio[0] - cp) * R(1.0 / TAUPI / 2.) + (cio[1] - cp) * R(1.0 / TAUPI / 2.) +
-                         xire - icat1;
-      const R rdth95 = R(0.95 * 5.0 / a.dt);
+                         (cs0 - ci0) * R(1.0 / TAUSI / 2.) - (cs0 - ci1) * R(1.0 / TAUSI / 2.) +
+                         csdiff;
+      const R cp_const =
+          (ci0 - cp) * R(1.0 / TAUPI / 2.) + (ci1 - cp) * R(1.0 / TAUPI / 2.) + xire - icat1;
 #pragma unroll 1
       for (int it = 0; it < 5; ++it) {
         const R r_sar = buffer_rate<R>(R(KSARON), R(KSAROFF), R(BSAR), casar, csn, dth, rdth95);
-        const R r_sarh = buffer_rate<R>(R(KSARHON), R(KSARHOFF), R(BSARH), casarh, csn, dth, rdth95);
+        const R r_sarh =
+            buffer_rate<R>(R(KSARHON), R(KSARHOFF), R(BSARH), casarh, csn, dth, rdth95);
         const R dotcs = R(VP / VS / TAUPS) * (cp - csn) + cs_const - (r_sar + r_sarh);
         const R cpbuff = buffer_rate<R>(R(KSARON), R(KSAROFF), R(BSAR), casarj, cp, dth, rdth95);
-        const R cpbuffh = buffer_rate<R>(R(KSARHON), R(KSARHOFF), R(BSARH), casarhj, cp, dth, rdth95);
+        const R cpbuffh =
+            buffer_rate<R>(R(KSARHON), R(KSARHOFF), R(BSARH), casarhj, cp, dth, rdth95);
         const R cpdot = (csn - cp) * R(1.0 / TAUPS) + cp_const - cpbuff - cpbuffh;
         casarj = clamp0(casarj + cpbuff * dth);
         casarhj = clamp0(casarhj + cpbuffh * dth);
@@ -542,7 +603,7 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs<R> a) {
     p_xicat = icat1;
     p_xinaca = xinaca;
 
-    if (out_step) {
+    if (OUT && out_step) {
       o[O_CP - P_STEP_END] = (double)cp;
       o[O_CJSR - P_STEP_END] = (double)cjsr;
       o[O_CJSRB - P_STEP_END] = (double)cjsrb;
@@ -583,15 +644,16 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs<R> a) {
           }
         }
 #pragma unroll
-        for (int k = 0; k < 7; ++k) o[O_TN1 - P_STEP_END + k] = tn[k];
+        for (int kk = 0; kk < 7; ++kk) o[O_TN1 - P_STEP_END + kk] = tn[kk];
       }
       o[O_SPARK - P_STEP_END] = nspark;
       o[O_CIHIGH - P_STEP_END] = ci_high ? 1.0 : 0.0;
-      if (y == sc.line_y && z == sc.line_z) {  // linescan row (:967-989)
-        double* r = a.out_ls + ((size_t)sc.ls_off + (size_t)s_slot * lx + x) * RH_LINESCAN_COLS;
-        r[0] = sv.t;
+      if (y == sh.line_y && z == sh.line_z) {  // linescan row (:967-989), post-step values
+        const int64_t g0 = g;
+        double* r = a.out_ls + ((size_t)sh.ls_off + (size_t)sh.slot * lx + x) * RH_LINESCAN_COLS;
+        r[0] = sh.t;
         r[1] = (double)(x + 1);
-        r[2] = (double)ci_sub0;
+        r[2] = (double)cinext2[g0].x;
         r[3] = nob;
         r[4] = nou;
         r[5] = ncb;
@@ -601,12 +663,12 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs<R> a) {
         r[9] = (double)cp;
         r[10] = (double)casar;
         r[11] = (double)casarh;
-        r[12] = (double)camyo0;
-        r[13] = (double)mgmyo0;
-        r[14] = (double)casr0;
-        r[15] = (double)cacal0;
-        r[16] = (double)cats0;
-        r[17] = (double)catf0;
+        r[12] = (double)L.camyo[2 * g0];
+        r[13] = (double)L.mgmyo[2 * g0];
+        r[14] = (double)L.casr[2 * g0];
+        r[15] = (double)L.cacal[2 * g0];
+        r[16] = (double)L.cats[2 * g0];
+        r[17] = (double)L.catf[2 * g0];
         r[18] = (double)xire;
         r[19] = (double)cjsr;
         r[20] = (double)ancx;
@@ -616,7 +678,7 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs<R> a) {
   }
 
   // ---- CTA reduction of the partials ----
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = tid >> 5, lane = tid & 31;
   {
     double s, c;
     warp_sum_comp(p_cs, s, c);
@@ -634,22 +696,22 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs<R> a) {
       s_red[warp][P_XINACA] = s;
       s_red[warp][P_XINACA + 1] = c;
     }
-    if (out_step) {
+    if (OUT && out_step) {
 #pragma unroll 1
-      for (int k = 0; k < NOUT; ++k) {
-        double v = o[k];
-        if (k == O_CIHIGH - P_STEP_END) {
+      for (int kk = 0; kk < NOUT; ++kk) {
+        double v = o[kk];
+        if (kk == O_CIHIGH - P_STEP_END) {
 #pragma unroll
           for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
         } else {
           v = warp_sum(v);
         }
-        if (lane == 0) s_red[warp][P_STEP_END + k] = v;
+        if (lane == 0) s_red[warp][P_STEP_END + kk] = v;
       }
     }
   }
   __syncthreads();
-  if (threadIdx.x < 32) {
+  if (tid < 32) {
     constexpr int NW = kBlock / 32;
     double* dst = a.partials + (size_t)blockIdx.x * P_COUNT;
     if (lane < 3) {
@@ -664,41 +726,35 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs<R> a) {
       dst[2 * lane] = s;
       dst[2 * lane + 1] = c;
     }
-    if (out_step) {
-      for (int k = lane; k < NOUT; k += 32) {
+    if (OUT && out_step) {
+      for (int kk = lane; kk < NOUT; kk += 32) {
         double v = 0.0;
-        if (k == O_CIHIGH - P_STEP_END) {
-          for (int w = 0; w < NW; ++w) v = fmax(v, s_red[w][P_STEP_END + k]);
+        if (kk == O_CIHIGH - P_STEP_END) {
+          for (int w = 0; w < NW; ++w) v = fmax(v, s_red[w][P_STEP_END + kk]);
         } else {
-          for (int w = 0; w < NW; ++w) v += s_red[w][P_STEP_END + k];
+          for (int w = 0; w < NW; ++w) v += s_red[w][P_STEP_END + kk];
         }
-        dst[P_STEP_END + k] = v;
+        dst[P_STEP_END + kk] = v;
       }
     }
+    __syncwarp();
     if (lane == 0) {
       if (s_status) atomicOr(&a.dyn[cell].status, s_status);
       __threadfence();
       unsigned int prev = atomicAdd(&a.dyn[cell].arrive, 1u);
-      s_last = (prev == (unsigned)(sc.tile_count - 1));
+      s_last = (prev == (unsigned)(sh.tile_count - 1));
     }
     __syncwarp();
   }
   __syncthreads();
   if (!s_last) return;
   // ---- last CTA of the cell: whole-cell update ----
-  if (threadIdx.x < 32) {
+  if (tid < 32) {
     __threadfence();
-    if (a.lattice_only) {
-      if (threadIdx.x == 0) {
-        a.dyn[cell].parity = par ^ 1;
-        a.dyn[cell].arrive = 0;
-      }
-    } else {
-      cell_update<R>(a, cell, sc, out_step);
-      if (threadIdx.x == 0) {
-        a.dyn[cell].parity = par ^ 1;
-        a.dyn[cell].arrive = 0;
-      }
+    if (!a.lattice_only) cell_update<R>(a, cell, out_step);
+    if (tid == 0) {
+      a.dyn[cell].parity = par ^ 1;
+      a.dyn[cell].arrive = 0;
     }
   }
 }
@@ -726,7 +782,7 @@ __global__ void init_kernel(Lattice<R> L, const CellConst* cells, const InitValu
     L.casarj[g] = R(v.casarj);
     L.casarhj[g] = R(v.casarhj);
     for (int ii = 0; ii < 8; ++ii) {
-      const int64_t gi = ii * S + g;
+      const int64_t gi = sub_index(ii, g, S);
       L.ci[0][gi] = R(v.ci);
       L.ci[1][gi] = R(v.ci);
       L.cnsr[0][gi] = R(v.cnsr);
@@ -745,15 +801,18 @@ __global__ void init_kernel(Lattice<R> L, const CellConst* cells, const InitValu
   }
 }
 
-// Voltage coefficients from the current membrane state (after create or a
-// host-side membrane change).
-__global__ void volt_prep_kernel(const CellConst* cells, CellDyn* dyn, int ncells, double dt) {
+// Coefficients of the next lattice update from the current membrane state
+// (after create or a host-side membrane change).
+__global__ void coef_prep_kernel(const CellConst* cells, CellDyn* dyn, int ncells, double dt) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
-  VoltCoef vc;
-  volt_coef(vc, dyn[c].m, cells[c], dt);
-  dyn[c].vc = vc;
-  if (!vc.active) {
+  StepCoef<double> kd;
+  bool active = step_coef(kd, dyn[c].m, cells[c], dt);
+  StepCoef<float> kf;
+  convert_coef(kf, kd);
+  dyn[c].cd = kd;
+  dyn[c].cf = kf;
+  if (!active) {
     dyn[c].done = 1;
     dyn[c].status |= RH_STATUS_DONE;
   } else {
@@ -785,7 +844,7 @@ cudaError_t launch_init(const Lattice<R>& L, const CellConst* cells, const InitV
 
 cudaError_t launch_volt_prep(const CellConst* cells, CellDyn* dyn, int ncells, double dt,
                              cudaStream_t st) {
-  volt_prep_kernel<<<(ncells + 127) / 128, 128, 0, st>>>(cells, dyn, ncells, dt);
+  coef_prep_kernel<<<(ncells + 127) / 128, 128, 0, st>>>(cells, dyn, ncells, dt);
   return cudaGetLastError();
 }
 

@@ -9,6 +9,13 @@ namespace rh {
 
 // CRUs (threads) per CTA of the step kernel.
 constexpr int kBlock = 128;
+// Resident CTAs per SM the register allocation is bounded for: the FP32
+// kernel is latency-bound and wants warps; the FP64 kernel is bound by the
+// FP64 pipe and wants registers (no spills).
+template <class R>
+constexpr int min_blocks() {
+  return sizeof(R) == 4 ? 5 : 3;
+}
 
 // Basal values of one cell (Init kernel, cuda_Cell_Detailed.cu:1121-1174),
 // computed on the host in FP64 and broadcast to every CRU of the cell.

@@ -54,14 +54,35 @@ def test_fp64_single_step_bitexact_counts(variant):
     assert worst[1] <= FP64_RTOL, errs
 
 
+def _gaussian_branch_crus(st, ku, ku2, kb, dt=0.025):
+    """CRUs whose CU->OU (pkum) or OB->OU (pbu) transition takes the Gaussian
+    branch of subroutine_cuda.c:336/447 (n > 5 and p >= 0.3, or n > 1 and
+    p >= 0.2 ... evaluated as the reference does)."""
+    cp, cj = st["cp"], st["cjsr"]
+    common = 1 / ((1 + (5000 / cj) ** 2) * (1 + (ku / cp) ** 2))
+    pku = np.minimum(4.5 * 1.5 * ku2 * common, 1 / dt)
+    pkb = np.minimum(4.5 * 1.5 / 36 * kb * common, 1 / dt)
+    pkum = pku * dt
+    pbu = (1 / 220.0) * dt * (pku / pkb)
+
+    def gauss(n, p):
+        return ~((n <= 1) | (p < 0.2) | ((n <= 5) & (p < 0.3)))
+    return gauss(st["ncu"], pkum) | gauss(st["nob"], pbu)
+
+
 def test_fp64_single_step_gaussian_branches_exercised():
-    """The hot CRUs must drive the Gaussian RyR branch (pkum >= 0.2 with
-    ncu > 5): check it on the oracle's inputs, then parity."""
-    p = c1_params(ku=1.0, ku2=3.0)
-    st, m = rich_state(p, hot_frac=0.4, seed=3)
-    cp, cj, ncu = st["cp"], st["cjsr"], st["ncu"]
-    pku = 4.5 * 1.5 * 3.0 / ((1 + (5000 / cj) ** 2) * (1 + (1.0 / cp) ** 2))
-    assert np.sum((pku * 0.025 >= 0.2) & (ncu > 5)) > 10
+    """Gaussian RyR draws (Box-Muller with a dither bit) are reached when the
+    bound-RyR reopening rate dominates (Ku2/Kb large) or the JSR is
+    overloaded; build such CRUs, check on the oracle's inputs that the branch
+    is taken, then require parity."""
+    ku, ku2, kb = 1.0, 3.0, 0.01
+    p = c1_params(ku=ku, ku2=ku2, kb=kb)
+    st, m = rich_state(p, hot_frac=0.5, seed=3)
+    rng = np.random.default_rng(4)
+    over = rng.choice(st.n, st.n // 5, replace=False)
+    st["cjsr"][over] = rng.uniform(5000.0, 9000.0, over.size)
+    g = _gaussian_branch_crus(st, ku, ku2, kb)
+    assert g.sum() > 20, g.sum()
     ref = _oracle_lattice_step(p, st, m)
     got = _gpu_lattice_step(p, st, m, "fp64")
     assert not count_mismatch(got, ref).any()
