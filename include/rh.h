@@ -60,6 +60,9 @@ extern "C" {
                                          Gaussian draw is then NaN, is redrawn up to
                                          the 200-try cap and counts 0 */
 
+#define RH_STATUS_TIMEOUT 0x20u       /* a bounded wait for a tile's bulk copies ran
+                                         out; that tile was not updated */
+
 /* Number of columns of one wholecell record and one linescan row. */
 #define RH_WHOLECELL_COLS 45
 #define RH_LINESCAN_COLS 22
@@ -192,6 +195,14 @@ int rh_drain_linescan(rh_sim* sim, int32_t cell, double* rows, int32_t max_rec,
                       int32_t* nrec);
 int rh_drain_stats(rh_sim* sim, int32_t cell, rh_beat_stats* out, int32_t max_rec,
                    int32_t* nrec);
+
+/* Per-beat statistics of a recorded trace, with the same detectors the
+ * simulator runs on the GPU (for traces produced elsewhere, e.g. by a CPU
+ * model): t and v are the per-step (time, membrane voltage after the step)
+ * samples, wholecell the output records of the same run.  Host-only. */
+int rh_analyze_trace(double pcl_ms, const double* t, const double* v, int64_t nsteps,
+                     const double* wholecell, int32_t nrec, rh_beat_stats* out, int32_t max_rec,
+                     int32_t* nbeats);
 
 /* Status bits of a cell (RH_STATUS_*). */
 int rh_cell_status(rh_sim* sim, int32_t cell, uint32_t* status);

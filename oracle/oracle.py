@@ -50,6 +50,10 @@ def lib() -> C.CDLL:
                               C.POINTER(C.c_int32)]
         L.orc_run.restype = C.c_int64
         L.orc_lattice_step.argtypes = [C.c_void_p]
+        L.orc_run_traced.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32,
+                                     C.POINTER(C.c_int32)]
+        L.orc_run_traced.restype = C.c_int64
         L.orc_get_state.argtypes = [C.c_void_p, C.POINTER(StateF64)]
         L.orc_set_state.argtypes = [C.c_void_p, C.POINTER(StateF64)]
         L.orc_get_membrane.argtypes = [C.c_void_p, C.POINTER(Membrane)]
@@ -124,6 +128,18 @@ class Oracle:
         done = self.L.orc_run(self.h, int(nsteps), _dptr(wc), max_rec, C.byref(nrec), _dptr(ls),
                               max_rec, C.byref(nbl))
         return done, wc[: nrec.value].copy(), ls[: nbl.value].copy()
+
+    def run_traced(self, nsteps: int):
+        """Runs nsteps; returns (t[n], v[n], wholecell[nrec,45]) where t is each
+        step's time before the step and v the voltage after it."""
+        t = np.zeros(nsteps)
+        v = np.zeros(nsteps)
+        max_rec = nsteps // 100 + 2
+        wc = np.zeros((max_rec, WHOLECELL_COLS))
+        nrec = C.c_int32(0)
+        done = self.L.orc_run_traced(self.h, int(nsteps), _dptr(t), _dptr(v), _dptr(wc), max_rec,
+                                     C.byref(nrec))
+        return t[:done].copy(), v[:done].copy(), wc[: nrec.value].copy()
 
     def get_state(self) -> HostState:
         hs = HostState(self.n)

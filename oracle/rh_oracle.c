@@ -1125,6 +1125,25 @@ int64_t orc_run(orc_sim* s, int64_t nsteps, double* wholecell, int32_t max_rec, 
   return done;
 }
 
+int64_t orc_run_traced(orc_sim* s, int64_t nsteps, double* t_out, double* v_out,
+                       double* wholecell, int32_t max_rec, int32_t* nrec) {
+  int64_t done = 0;
+  int32_t nr = 0;
+  while (done < nsteps && s->m.t < s->tend) {
+    double t0 = s->m.t;
+    int out = orc_step(s);
+    if (t_out) t_out[done] = t0;
+    if (v_out) v_out[done] = s->m.v;
+    if (out && wholecell && nr < max_rec) {
+      memcpy(wholecell + (size_t)nr * RH_WHOLECELL_COLS, s->wc, sizeof(s->wc));
+      nr++;
+    }
+    done++;
+  }
+  if (nrec) *nrec = nr;
+  return done;
+}
+
 /* ------------------------------ construction ----------------------------- */
 
 orc_sim* orc_create(const rh_cell_params* p, double dt) {

@@ -44,6 +44,11 @@ int orc_step(orc_sim* s);
 int64_t orc_run(orc_sim* s, int64_t nsteps, double* wholecell, int32_t max_rec,
                 int32_t* nrec, double* linescan, int32_t max_blocks, int32_t* nblocks);
 
+/* As orc_run, also recording each step's time (before the step) and
+ * membrane voltage (after it): the samples the per-beat detectors use. */
+int64_t orc_run_traced(orc_sim* s, int64_t nsteps, double* t_out, double* v_out,
+                       double* wholecell, int32_t max_rec, int32_t* nrec);
+
 /* Lattice update only (Compute + ping-pong swap) with the current v, t, xnai. */
 void orc_lattice_step(orc_sim* s);
 

@@ -17,6 +17,7 @@ RH_STATUS_GAUSS_RETRY = 0x2
 RH_STATUS_CI_HIGH = 0x4
 RH_STATUS_DONE = 0x8
 RH_STATUS_RATE_CAP = 0x10
+RH_STATUS_TIMEOUT = 0x20
 WHOLECELL_COLS = 45
 LINESCAN_COLS = 22
 

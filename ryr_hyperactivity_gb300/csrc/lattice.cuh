@@ -22,6 +22,7 @@
 #include <stdint.h>
 
 #include "../../include/rh.h"
+#include "beatstats.cuh"
 #include "model.cuh"
 
 namespace rh {
@@ -70,19 +71,6 @@ struct CellConst {
   double svica, svncx, sviup_tot, svikr, cao, ku, ku2, kb, pcl, tend;
 };
 
-// Per-beat statistics tracker (project-defined detectors; see stats in step.cu).
-struct BeatTracker {
-  int beat;            // current beat index
-  int ead;
-  double t_beat0;      // stimulus onset of the current beat
-  double v_rest, v_peak, t_peak, v_min_after_peak;
-  double apd90;
-  double ci_peak, sr_load;
-  int sparks;
-  int phase;           // 0 before upstroke, 1 depolarised, 2 repolarised
-  long long count;     // beats completed
-};
-
 // Mutable per-cell state, owned by the device between host calls.
 struct CellDyn {
   rh_membrane m;
@@ -93,7 +81,8 @@ struct CellDyn {
   int done;
   unsigned int arrive;  // CTAs of this cell that finished the current step
   long long out_count;  // output records produced
-  BeatTracker bt;
+  BeatTracker bt;       // per-beat statistics in progress
+  long long stats_count;  // beat records produced
 };
 
 // Quantities each CTA reduces over its CRUs.  The first three are needed
@@ -136,6 +125,8 @@ struct StepArgs {
   double* out_wc;     // [cell][cap][45]
   double* out_ls;     // [ls_off + slot*lx + x][22]
   double* diag;       // optional
+  rh_beat_stats* stats;  // [cell][stats_cap], optional
+  int stats_cap;
   int out_cap;
   int lattice_only;
   double dt;

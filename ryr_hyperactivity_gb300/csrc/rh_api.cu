@@ -45,11 +45,12 @@ struct rh_sim {
   double* d_out_wc = nullptr;
   double* d_out_ls = nullptr;
   double* d_diag = nullptr;
+  rh_beat_stats* d_stats = nullptr;
   int64_t ls_rows_total = 0;
   // host mirror of each cell's clock (same IEEE additions as the device)
   std::vector<double> t_host;
   std::vector<char> active_host;
-  std::vector<long long> drained_wc, drained_ls;
+  std::vector<long long> drained_wc, drained_ls, drained_st;
   // graphs keyed by (window length, output-step bitmask)
   std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
   // timing
@@ -185,6 +186,8 @@ void carve(Lattice<R>& L, char*& p, int64_t S) {
 
 size_t lattice_bytes(size_t rs, int64_t S) {
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  // 10 per-CRU real fields (cs twice), 10 sub-voxel fields (8 values per CRU,
+  // ci and cnsr twice), packed integers
   return 10 * al(S * rs) + 10 * al(8 * S * rs) + al(S * 4) + al(S * 8) + al(S * 4);
 }
 
@@ -199,6 +202,8 @@ StepArgs<R> make_args(rh_sim* s, const Lattice<R>& L, bool lattice_only) {
   a.out_wc = s->d_out_wc;
   a.out_ls = s->d_out_ls;
   a.diag = (lattice_only || s->opts.keep_diagnostics) ? s->d_diag : nullptr;
+  a.stats = s->d_stats;
+  a.stats_cap = s->opts.stats_capacity;
   a.out_cap = s->opts.output_capacity;
   a.lattice_only = lattice_only ? 1 : 0;
   a.dt = s->opts.dt_ms;
@@ -342,6 +347,7 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   else rh_default_run_opts(&s->opts);
   if (s->opts.output_capacity <= 0) s->opts.output_capacity = 64;
   if (s->opts.window_steps <= 0) s->opts.window_steps = 100;
+  if (s->opts.stats_capacity <= 0) s->opts.stats_capacity = 64;
   if (!(s->opts.dt_ms > 0)) return fail(s, RH_ERR_ARG, "dt_ms must be positive");
   if (s->opts.precision != RH_FP64 && s->opts.precision != RH_MIXED)
     return fail(s, RH_ERR_ARG, "unknown precision %d", s->opts.precision);
@@ -368,7 +374,8 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     cc.n = (int)n64;
     cc.off = off;
     cc.tile_begin = tiles;
-    cc.tile_count = (cc.n + kBlock - 1) / kBlock;
+    const int kb = s->opts.precision == RH_MIXED ? block_of<float>() : block_of<double>();
+    cc.tile_count = (cc.n + kb - 1) / kb;
     int jz = p.linescan_jz < 0 ? 5 : p.linescan_jz;
     if (jz > p.nz - 2) jz = p.nz / 2;
     if (jz < 1) jz = 1;
@@ -393,7 +400,7 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     cc.pcl = p.pcl_ms;
     cc.tend = p.nbeats * p.pcl_ms + 2100;
     for (int t = 0; t < cc.tile_count; ++t)
-      s->htiles.push_back(make_int4(c, t * kBlock, std::min(kBlock, cc.n - t * kBlock), 0));
+      s->htiles.push_back(make_int4(c, t * kb, std::min(kb, cc.n - t * kb), 0));
     tiles += cc.tile_count;
     off += (n64 + 31) & ~int64_t(31);
     ls_off += (int64_t)s->opts.output_capacity * cc.lx;
@@ -424,6 +431,8 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   CK(cudaMalloc(&s->d_out_wc, sizeof(double) * RH_WHOLECELL_COLS * (size_t)ncells *
                                   s->opts.output_capacity));
   CK(cudaMalloc(&s->d_out_ls, sizeof(double) * RH_LINESCAN_COLS * (size_t)std::max<int64_t>(ls_off, 1)));
+  if (s->opts.track_stats)
+    CK(cudaMalloc(&s->d_stats, sizeof(rh_beat_stats) * (size_t)ncells * s->opts.stats_capacity));
   CK(cudaMemcpyAsync(s->d_cells, s->hcells.data(), sizeof(CellConst) * ncells,
                      cudaMemcpyHostToDevice, s->stream));
   CK(cudaMemcpyAsync(s->d_tiles, s->htiles.data(), sizeof(int4) * tiles, cudaMemcpyHostToDevice,
@@ -435,10 +444,12 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   s->active_host.resize(ncells);
   s->drained_wc.assign(ncells, 0);
   s->drained_ls.assign(ncells, 0);
+  s->drained_st.assign(ncells, 0);
   for (int c = 0; c < ncells; ++c) {
     iv[c] = init_values(cells[c]);
     memset(&dyn[c], 0, sizeof(CellDyn));
     dyn[c].m = initial_membrane(cells[c]);
+    beat_reset(dyn[c].bt);
     s->t_host[c] = dyn[c].m.t;
     s->active_host[c] = dyn[c].m.t < s->hcells[c].tend;
   }
@@ -473,6 +484,7 @@ int rh_destroy(rh_sim* s) {
   cudaFree(s->d_out_wc);
   cudaFree(s->d_out_ls);
   cudaFree(s->d_diag);
+  cudaFree(s->d_stats);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -826,10 +838,49 @@ int rh_drain_linescan(rh_sim* s, int32_t cell, double* rows, int32_t max_rec, in
 int rh_drain_stats(rh_sim* s, int32_t cell, rh_beat_stats* out, int32_t max_rec, int32_t* nrec) {
   int r = check_cell(s, cell);
   if (r) return r;
-  if (!nrec) return RH_ERR_ARG;
-  (void)out;
-  (void)max_rec;
+  if (!nrec || max_rec < 0 || (max_rec > 0 && !out)) return RH_ERR_ARG;
   *nrec = 0;
+  if (!s->d_stats) return RH_OK;
+  CK(cudaSetDevice(s->device));
+  CellDyn d;
+  if ((r = read_dyn(s, cell, &d))) return r;
+  const int cap = s->opts.stats_capacity;
+  long long first = s->drained_st[cell];
+  if (d.stats_count - first > cap) first = d.stats_count - cap;
+  int cnt = (int)std::min<long long>(d.stats_count - first, max_rec);
+  for (int k = 0; k < cnt; ++k) {
+    long long slot = (first + k) % cap;
+    CK(cudaMemcpy(out + k, s->d_stats + (size_t)cell * cap + slot, sizeof(rh_beat_stats),
+                  cudaMemcpyDeviceToHost));
+  }
+  s->drained_st[cell] = first + cnt;
+  *nrec = cnt;
+  return RH_OK;
+}
+
+int rh_analyze_trace(double pcl_ms, const double* t, const double* v, int64_t nsteps,
+                     const double* wholecell, int32_t nrec, rh_beat_stats* out, int32_t max_rec,
+                     int32_t* nbeats) {
+  if (!t || !v || !nbeats || nsteps < 0 || nrec < 0 || (nrec > 0 && !wholecell) ||
+      !(pcl_ms > 0) || max_rec < 0 || (max_rec > 0 && !out))
+    return RH_ERR_ARG;
+  BeatTracker b;
+  beat_reset(b);
+  int32_t nb = 0, rec = 0;
+  for (int64_t i = 0; i < nsteps; ++i) {
+    rh_beat_stats st;
+    if (beat_on_step(b, t[i], v[i], pcl_ms, &st)) {
+      if (nb < max_rec) out[nb] = st;
+      ++nb;
+    }
+    // output records carry the step time in column 1
+    while (rec < nrec && wholecell[(size_t)rec * RH_WHOLECELL_COLS] <= t[i]) {
+      if (wholecell[(size_t)rec * RH_WHOLECELL_COLS] == t[i])
+        beat_on_output(b, wholecell + (size_t)rec * RH_WHOLECELL_COLS);
+      ++rec;
+    }
+  }
+  *nbeats = std::min(nb, max_rec);
   return RH_OK;
 }
 
@@ -911,6 +962,7 @@ int rh_restore(rh_sim* s, const char* path) {
     s->active_host[c] = !dyn[c].done;
     s->drained_wc[c] = dyn[c].out_count;
     s->drained_ls[c] = dyn[c].out_count;
+    s->drained_st[c] = dyn[c].stats_count;
   }
   return RH_OK;
 }
@@ -949,6 +1001,7 @@ int rh_import_state(rh_sim* s, const void* host, size_t bytes) {
     s->active_host[c] = !dyn[c].done;
     s->drained_wc[c] = std::min(s->drained_wc[c], dyn[c].out_count);
     s->drained_ls[c] = std::min(s->drained_ls[c], dyn[c].out_count);
+    s->drained_st[c] = std::min(s->drained_st[c], dyn[c].stats_count);
   }
   CK(cudaStreamSynchronize(s->stream));
   return RH_OK;
@@ -956,8 +1009,9 @@ int rh_import_state(rh_sim* s, const void* host, size_t bytes) {
 
 int rh_bytes_per_cru_step(const rh_sim* s, double* bytes) {
   if (!s || !bytes) return RH_ERR_ARG;
-  // 73 persistent real fields + 16 B of packed integers, each read and written once
-  *bytes = 2.0 * (73.0 * (double)real_size(s)) + 2.0 * 16.0;
+  // 73 persistent real fields and 16 B of packed integers, each read and
+  // written once
+  *bytes = 2.0 * (73.0 * (double)real_size(s) + 16.0);
   return RH_OK;
 }
 

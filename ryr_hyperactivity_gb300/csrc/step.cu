@@ -134,12 +134,20 @@ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step) {
   if (!isfinite(m.v) || !isfinite(m.xnai) || !isfinite(m.csubt) || !isfinite(m.xicatto) ||
       !isfinite(m.xinacato))
     status |= RH_STATUS_NAN;
+  if (a.stats) {  // per-beat detectors on the (t, V) sample of this step
+    rh_beat_stats rec;
+    if (beat_on_step(dyn->bt, m.t, m.v, cc.pcl, &rec)) {
+      a.stats[(size_t)cell * a.stats_cap + dyn->stats_count % a.stats_cap] = rec;
+      dyn->stats_count += 1;
+    }
+  }
   if (out_step) {
     m.sparksum += (long long)osum[O_SPARK - P_STEP_END];
     if (osum[O_CIHIGH - P_STEP_END] > 0) status |= RH_STATUS_CI_HIGH;
     long long slot = dyn->out_count % a.out_cap;
     double* w = a.out_wc + ((size_t)cell * a.out_cap + slot) * RH_WHOLECELL_COLS;
     wholecell_columns(w, osum, m, cc.n, dt);
+    if (a.stats) beat_on_output(dyn->bt, w);
     dyn->out_count += 1;
     m.sparksum = 0;  // :1074-1077
     m.out_ica = 0;
@@ -173,7 +181,8 @@ struct TileHeader {
 };
 
 template <class R, bool OUT>
-__global__ void __launch_bounds__(kBlock, min_blocks<R>()) step_kernel(StepArgs<R> a) {
+__global__ void __launch_bounds__(block_of<R>(), min_blocks<R>()) step_kernel(StepArgs<R> a) {
+  constexpr int kBlock = block_of<R>();
   __shared__ TileHeader sh;
   __shared__ StepCoef<R> sk;
   using V = typename Vec2<R>::T;
@@ -827,9 +836,9 @@ template <class R>
 cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, cudaStream_t st) {
   if (ntiles <= 0) return cudaSuccess;
   if (out)
-    step_kernel<R, true><<<ntiles, kBlock, 0, st>>>(a);
+    step_kernel<R, true><<<ntiles, block_of<R>(), 0, st>>>(a);
   else
-    step_kernel<R, false><<<ntiles, kBlock, 0, st>>>(a);
+    step_kernel<R, false><<<ntiles, block_of<R>(), 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -8,12 +8,17 @@
 namespace rh {
 
 // CRUs (threads) per CTA of the step kernel.
-constexpr int kBlock = 128;
-// Resident CTAs per SM the register allocation is bounded for: the FP32
-// kernel is latency-bound and wants warps; the FP64 kernel is bound by the
-// FP64 pipe and wants registers (no spills).
 template <class R>
-constexpr int min_blocks() {
+__host__ __device__ constexpr int block_of() {
+  return 128;
+}
+
+// Resident CTAs per SM the register allocation is bounded for: the FP32
+// kernel is latency-bound and wants warps (5 x 128 threads at <= 102
+// registers measured best); the FP64 kernel is bound by the FP64 pipe and
+// wants registers.
+template <class R>
+__host__ __device__ constexpr int min_blocks() {
   return sizeof(R) == 4 ? 5 : 3;
 }
 

@@ -1,0 +1,58 @@
+// tma.cuh — bulk asynchronous copies (the TMA unit's 1-D cp.async.bulk) from
+// global to shared memory, completed on an mbarrier, with bounded waits.
+//
+// Rules kept here: both addresses 16-byte aligned, sizes multiples of 16
+// bytes, the mbarrier initialised and fenced before any copy names it, and
+// every wait gives up after a fixed number of polls (the caller records the
+// timeout and never reads the buffers).
+#pragma once
+
+#include <stdint.h>
+
+namespace rh {
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// global -> shared bulk copy of `bytes` (multiple of 16, both ends 16-byte
+// aligned), signalling `bar` with the transferred byte count
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Polls the barrier's phase `parity` at most `max_polls` times; returns 1 when
+// the phase completed, 0 on timeout.
+__device__ __forceinline__ int mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_polls) {
+  const uint32_t a = smem_addr(bar);
+  for (uint32_t i = 0; i < max_polls; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return 1;
+  }
+  return 0;
+}
+
+}  // namespace rh

@@ -20,6 +20,7 @@ EXPORTS = [
     "rh_drain_linescan", "rh_drain_stats", "rh_cell_status", "rh_checkpoint", "rh_restore",
     "rh_bytes_per_cru_step", "rh_kernel_timing", "rh_last_error", "rh_format_wholecell",
     "rh_format_linescan", "rh_state_bytes", "rh_export_state", "rh_import_state",
+    "rh_analyze_trace",
 ]
 
 _lib = None
@@ -58,6 +59,8 @@ def load() -> C.CDLL:
     L.rh_drain_stats.argtypes = [vp, C.c_int32, C.POINTER(BeatStats), C.c_int32,
                                  C.POINTER(C.c_int32)]
     L.rh_cell_status.argtypes = [vp, C.c_int32, C.POINTER(C.c_uint32)]
+    L.rh_analyze_trace.argtypes = [C.c_double, dp, dp, C.c_int64, dp, C.c_int32,
+                                   C.POINTER(BeatStats), C.c_int32, C.POINTER(C.c_int32)]
     L.rh_checkpoint.argtypes = [vp, C.c_char_p]
     L.rh_restore.argtypes = [vp, C.c_char_p]
     L.rh_bytes_per_cru_step.argtypes = [vp, dp]

@@ -159,6 +159,24 @@ class Simulator:
         return n.value, ms.value
 
 
+def analyze_trace(pcl_ms: float, t, v, wholecell, max_beats: int = 4096) -> list[dict]:
+    """Per-beat statistics of a (t, V) trace and its output records, computed
+    by the same detectors the simulator runs on the GPU."""
+    L = native.load()
+    t = np.ascontiguousarray(t, np.float64)
+    v = np.ascontiguousarray(v, np.float64)
+    wc = np.ascontiguousarray(wholecell, np.float64).reshape(-1, WHOLECELL_COLS)
+    arr = (BeatStats * max_beats)()
+    n = C.c_int32()
+    dp = C.POINTER(C.c_double)
+    rc = L.rh_analyze_trace(float(pcl_ms), t.ctypes.data_as(dp), v.ctypes.data_as(dp), len(t),
+                            wc.ctypes.data_as(dp), len(wc), arr, max_beats, C.byref(n))
+    if rc != 0:
+        raise native.NativeError(f"rh_analyze_trace failed ({rc})")
+    return [{k: getattr(arr[i], k) for k, _ in BeatStats._fields_ if k != "pad"}
+            for i in range(n.value)]
+
+
 def format_wholecell(row) -> str:
     L = native.load()
     a = np.ascontiguousarray(row, np.float64)
