@@ -1,0 +1,54 @@
+/*
+ * rh_mlp.h — C ABI of the surrogate network that screens parameter sweeps.
+ *
+ * No counterpart in the reference (cuda_Cell_Detailed.cu has no learned
+ * component); the network is this project's addition: 4 inputs (RyR open-rate
+ * scale Ku2, IKr scale, PCL, [Ca]o, each normalised to [0, 1]) -> three
+ * hidden layers of 128 ReLU units -> 3 outputs (EAD probability, normalised
+ * APD90 mean, normalised APD90 variance).  BF16 weights and activations,
+ * FP32 accumulation on the tensor cores, FP32 master weights trained with
+ * Adam by the library's own forward and backward kernels.
+ *
+ * Parameter vector layout (floats): for layers 1..4, W (n x k, row-major)
+ * then b (n), with padded shapes W1 128x16 (inputs 4..15 zero), W2 128x128,
+ * W3 128x128, W4 8x128 (outputs 3..7 zero), b4 of 8.
+ * Status codes are those of rh.h.
+ */
+#ifndef RH_MLP_H
+#define RH_MLP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "rh.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RH_MLP_IN 4
+#define RH_MLP_OUT 3
+
+typedef struct rh_mlp rh_mlp;
+
+int rh_mlp_create(int32_t batch_max, int32_t device, rh_mlp** out);
+int rh_mlp_destroy(rh_mlp* m);
+int rh_mlp_param_count(const rh_mlp* m, int32_t* n);
+int rh_mlp_set_params(rh_mlp* m, const float* params);
+int rh_mlp_get_params(rh_mlp* m, float* params);
+/* y[n x 3] = network(x[n x 4]); any n (processed in batches of batch_max). */
+int rh_mlp_forward(rh_mlp* m, const float* x, int32_t n, float* y);
+/* Loss and parameter gradients for one batch (n <= batch_max); grads in the
+ * parameter layout (may be NULL). */
+int rh_mlp_gradients(rh_mlp* m, const float* x, const float* target, int32_t n, float* grads,
+                     float* loss);
+/* One Adam step (beta 0.9/0.999) on one batch; returns the batch loss. */
+int rh_mlp_train_step(rh_mlp* m, const float* x, const float* target, int32_t n, float lr,
+                      float* loss);
+int rh_mlp_last_error(const rh_mlp* m, char* buf, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

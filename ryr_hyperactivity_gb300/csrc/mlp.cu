@@ -1,0 +1,469 @@
+// mlp.cu — the surrogate network: 4 -> 128 -> 128 -> 128 -> 3, BF16 weights
+// and activations, FP32 accumulation and FP32 master weights (Adam).
+//
+// Outputs: y0 = sigmoid(z0) (EAD probability), y1 = z1 (normalised APD90
+// mean), y2 = softplus(z2) (normalised APD90 variance).  Loss per sample:
+// BCE(y0, p) + (y1 - m)^2 + (y2 - s)^2, averaged over the batch.
+//
+// Every GEMM runs on the tensor cores through one hand-written kernel
+// (mma.sync m16n8k16, BF16 x BF16 -> FP32): forward Z = A W^T, backward
+// dA = dZ W and dW = dZ^T A.  Padded shapes: layer 1 K = 16 (4 inputs +
+// zeros), layer 4 N = 8 (3 outputs + zeros).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/rh_mlp.h"
+
+namespace {
+
+constexpr int H = 128;   // hidden width
+constexpr int KIN = 16;  // padded input width
+constexpr int NOUT = 8;  // padded output width
+
+// C[M,N] (f32, row-major, ldc) = sum_k A(m,k) B(k,n); A(m,k) = A[m*sam + k*sak],
+// B(k,n) = Bm[k*sbk + n*sbn]; out-of-range elements read as zero.
+// One warp per 16 x 8 output tile.
+__global__ void gemm_bf16(const __nv_bfloat16* __restrict__ A, int sam, int sak,
+                          const __nv_bfloat16* __restrict__ Bm, int sbk, int sbn, float* C, int ldc,
+                          int M, int N, int K, int accumulate) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int tiles_n = (N + 7) / 8;
+  const int tm = warp / tiles_n, tn = warp % tiles_n;
+  if (tm * 16 >= M) return;
+  const int g = lane >> 2, tq = lane & 3;
+  const int m0 = tm * 16, n0 = tn * 8;
+  float c[4] = {0.f, 0.f, 0.f, 0.f};
+  auto ldA = [&](int m, int k) -> __nv_bfloat16 {
+    return (m < M && k < K) ? A[(int64_t)m * sam + (int64_t)k * sak] : __float2bfloat16(0.f);
+  };
+  auto ldB = [&](int k, int n) -> __nv_bfloat16 {
+    return (k < K && n < N) ? Bm[(int64_t)k * sbk + (int64_t)n * sbn] : __float2bfloat16(0.f);
+  };
+  auto pack = [](__nv_bfloat16 lo, __nv_bfloat16 hi) -> uint32_t {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+  };
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    const int ka = k0 + tq * 2;
+    uint32_t a0 = pack(ldA(m0 + g, ka), ldA(m0 + g, ka + 1));
+    uint32_t a1 = pack(ldA(m0 + g + 8, ka), ldA(m0 + g + 8, ka + 1));
+    uint32_t a2 = pack(ldA(m0 + g, ka + 8), ldA(m0 + g, ka + 9));
+    uint32_t a3 = pack(ldA(m0 + g + 8, ka + 8), ldA(m0 + g + 8, ka + 9));
+    uint32_t b0 = pack(ldB(ka, n0 + g), ldB(ka + 1, n0 + g));
+    uint32_t b1 = pack(ldB(ka + 8, n0 + g), ldB(ka + 9, n0 + g));
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+  }
+  const int r0 = m0 + g, r1 = m0 + g + 8, cc = n0 + tq * 2;
+  float* out[4] = {C + (int64_t)r0 * ldc + cc, C + (int64_t)r0 * ldc + cc + 1,
+                   C + (int64_t)r1 * ldc + cc, C + (int64_t)r1 * ldc + cc + 1};
+  const bool ok[4] = {r0 < M && cc < N, r0 < M && cc + 1 < N, r1 < M && cc < N,
+                      r1 < M && cc + 1 < N};
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (ok[q]) *out[q] = accumulate ? *out[q] + c[q] : c[q];
+}
+
+// Z += bias (per column); A = relu(Z) in BF16 (hidden layers).
+__global__ void bias_relu(float* Z, const float* bias, __nv_bfloat16* Aout, int M, int N) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)M * N) return;
+  float z = Z[i] + bias[i % N];
+  Z[i] = z;
+  Aout[i] = __float2bfloat16(z > 0.f ? z : 0.f);
+}
+
+__device__ __forceinline__ float sigmoidf_(float x) { return 1.f / (1.f + expf(-x)); }
+__device__ __forceinline__ float softplusf_(float x) { return x > 20.f ? x : log1pf(expf(x)); }
+
+// Output layer: y, loss terms and dZ4 (scaled by 1/B), in FP32 and BF16.
+__global__ void output_loss(float* Z4, const float* b4, const float* target, float* y,
+                            float* dz4, __nv_bfloat16* dz4b, float* loss_terms, int B) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B) return;
+  float z0 = Z4[i * NOUT + 0] + b4[0], z1 = Z4[i * NOUT + 1] + b4[1], z2 = Z4[i * NOUT + 2] + b4[2];
+  float y0 = sigmoidf_(z0), y1 = z1, y2 = softplusf_(z2);
+  y[i * 3 + 0] = y0;
+  y[i * 3 + 1] = y1;
+  y[i * 3 + 2] = y2;
+  float l = 0.f;
+  float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+  if (target) {
+    const float p = target[i * 3 + 0], m = target[i * 3 + 1], s = target[i * 3 + 2];
+    const float e = 1e-7f;
+    l = -(p * logf(fmaxf(y0, e)) + (1.f - p) * logf(fmaxf(1.f - y0, e))) + (y1 - m) * (y1 - m) +
+        (y2 - s) * (y2 - s);
+    const float invB = 1.f / (float)B;
+    g0 = (y0 - p) * invB;
+    g1 = 2.f * (y1 - m) * invB;
+    g2 = 2.f * (y2 - s) * sigmoidf_(z2) * invB;
+    loss_terms[i] = l;
+  }
+  const float gg[NOUT] = {g0, g1, g2, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int q = 0; q < NOUT; ++q) {
+    dz4[i * NOUT + q] = gg[q];
+    dz4b[i * NOUT + q] = __float2bfloat16(gg[q]);
+  }
+}
+
+// dZ = dA * relu'(Z) -> BF16
+__global__ void relu_backward(const float* dA, const float* Z, __nv_bfloat16* dZb, float* dZf,
+                              int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float d = Z[i] > 0.f ? dA[i] : 0.f;
+  dZf[i] = d;
+  dZb[i] = __float2bfloat16(d);
+}
+
+// db[n] = sum over rows of dZ (fixed order per column)
+__global__ void bias_grad(const float* dZ, float* db, int M, int N) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float s = 0.f;
+  for (int m = 0; m < M; ++m) s += dZ[(int64_t)m * N + n];
+  db[n] = s;
+}
+
+// Adam step on FP32 masters, refresh the BF16 copies.  Padded entries (mask
+// 0) stay zero.
+__global__ void adam_update(float* w, const float* g, float* m, float* v, __nv_bfloat16* wb,
+                            const float* mask, int n, float lr, float b1, float b2, float eps,
+                            float bc1, float bc2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (mask && mask[i] == 0.f) {
+    w[i] = 0.f;
+    if (wb) wb[i] = __float2bfloat16(0.f);
+    return;
+  }
+  float gi = g[i];
+  float mi = b1 * m[i] + (1.f - b1) * gi;
+  float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  w[i] = wi;
+  if (wb) wb[i] = __float2bfloat16(wi);
+}
+
+// inputs (B x 4 floats) -> padded BF16 rows of 16
+__global__ void pack_inputs(const float* x, __nv_bfloat16* X0, int B) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)B * KIN) return;
+  const int r = (int)(i / KIN), c = (int)(i % KIN);
+  X0[i] = __float2bfloat16(c < RH_MLP_IN ? x[r * RH_MLP_IN + c] : 0.f);
+}
+
+unsigned blocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+
+struct rh_mlp {
+  int bmax = 0;
+  cudaStream_t st = nullptr;
+  // parameters: FP32 masters, BF16 copies, Adam moments, gradients
+  float* P = nullptr;  // all FP32 buffers in one allocation
+  __nv_bfloat16* Pb = nullptr;
+  float *w[4], *b[4], *gw[4], *gb[4], *mw[4], *vw[4], *mb[4], *vb[4], *maskw[4];
+  __nv_bfloat16* wb[4];
+  int wn[4], wk[4];
+  // activations
+  __nv_bfloat16 *X0, *A[3], *dZb[4];
+  float *Z[4], *dA, *dZf, *y, *target, *xin, *loss;
+  int64_t step = 0;
+  std::string err;
+};
+
+namespace {
+
+int ck(rh_mlp* m, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return RH_OK;
+  if (m) m->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return RH_ERR_CUDA;
+}
+#define MCK(x)                                 \
+  do {                                         \
+    int r_ = ck(m, (x), #x);                   \
+    if (r_) return r_;                         \
+  } while (0)
+
+int gemm(rh_mlp* m, const __nv_bfloat16* A, int sam, int sak, const __nv_bfloat16* B, int sbk,
+         int sbn, float* C, int ldc, int M, int N, int K, int acc) {
+  const int tiles = ((M + 15) / 16) * ((N + 7) / 8);
+  gemm_bf16<<<blocks((int64_t)tiles * 32, 128), 128, 0, m->st>>>(A, sam, sak, B, sbk, sbn, C, ldc,
+                                                                 M, N, K, acc);
+  return ck(m, cudaGetLastError(), "gemm");
+}
+
+int forward(rh_mlp* m, int B) {
+  // layer l: Z = A_{l-1} W_l^T  (W_l stored n x k, row-major)
+  const __nv_bfloat16* in = m->X0;
+  int kin = KIN;
+  for (int l = 0; l < 3; ++l) {
+    int r = gemm(m, in, kin, 1, m->wb[l], 1, kin, m->Z[l], H, B, H, kin, 0);
+    if (r) return r;
+    bias_relu<<<blocks((int64_t)B * H, 256), 256, 0, m->st>>>(m->Z[l], m->b[l], m->A[l], B, H);
+    in = m->A[l];
+    kin = H;
+  }
+  return gemm(m, m->A[2], H, 1, m->wb[3], 1, H, m->Z[3], NOUT, B, NOUT, H, 0);
+}
+
+int backward(rh_mlp* m, int B) {
+  // output layer gradients were written by output_loss into dZf/dZb[3]
+  // dW4 = dZ4^T A3 ; db4 = sum dZ4 ; dA3 = dZ4 W4
+  int r;
+  const __nv_bfloat16* acts[4] = {m->X0, m->A[0], m->A[1], m->A[2]};
+  const int kins[4] = {KIN, H, H, H};
+  const int nouts[4] = {H, H, H, NOUT};
+  for (int l = 3; l >= 0; --l) {
+    const int N = nouts[l], K = kins[l];
+    // dW_l (N x K) = dZ_l^T (N x B) * A_{l-1} (B x K)
+    if ((r = gemm(m, m->dZb[l], 1, N, acts[l], K, 1, m->gw[l], K, N, K, B, 0))) return r;
+    if (l == 3) {
+      // dZ4 in FP32 lives in dA's first B*8 entries (written by output_loss)
+      bias_grad<<<blocks(N, 128), 128, 0, m->st>>>(m->dA, m->gb[l], B, N);
+    } else {
+      bias_grad<<<blocks(N, 128), 128, 0, m->st>>>(m->dZf, m->gb[l], B, N);
+    }
+    if (l == 0) break;
+    // dA_{l-1} (B x K) = dZ_l (B x N) * W_l (N x K)
+    if ((r = gemm(m, m->dZb[l], N, 1, m->wb[l], K, 1, m->dA, K, B, K, N, 0))) return r;
+    relu_backward<<<blocks((int64_t)B * K, 256), 256, 0, m->st>>>(m->dA, m->Z[l - 1], m->dZb[l - 1],
+                                                                m->dZf, (int64_t)B * K);
+  }
+  return ck(m, cudaGetLastError(), "backward");
+}
+
+int run_loss(rh_mlp* m, int B, const float* xh, const float* th, float* loss_out) {
+  MCK(cudaMemcpyAsync(m->xin, xh, sizeof(float) * RH_MLP_IN * B, cudaMemcpyHostToDevice, m->st));
+  if (th)
+    MCK(cudaMemcpyAsync(m->target, th, sizeof(float) * 3 * B, cudaMemcpyHostToDevice, m->st));
+  pack_inputs<<<blocks((int64_t)B * KIN, 256), 256, 0, m->st>>>(m->xin, m->X0, B);
+  int r = forward(m, B);
+  if (r) return r;
+  output_loss<<<blocks(B, 128), 128, 0, m->st>>>(m->Z[3], m->b[3], th ? m->target : nullptr, m->y,
+                                                 m->dA, m->dZb[3], m->loss, B);
+  MCK(cudaGetLastError());
+  if (loss_out && th) {
+    std::vector<float> l(B);
+    MCK(cudaMemcpyAsync(l.data(), m->loss, sizeof(float) * B, cudaMemcpyDeviceToHost, m->st));
+    MCK(cudaStreamSynchronize(m->st));
+    double s = 0;
+    for (float v : l) s += v;
+    *loss_out = (float)(s / B);
+  }
+  return RH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rh_mlp_create(int32_t batch_max, int32_t device, rh_mlp** out) {
+  if (!out || batch_max <= 0) return RH_ERR_ARG;
+  *out = nullptr;
+  rh_mlp* m = new rh_mlp();
+  m->bmax = batch_max;
+  const int wn[4] = {H, H, H, NOUT}, wk[4] = {KIN, H, H, H};
+  size_t nf = 0, nb = 0;
+  for (int l = 0; l < 4; ++l) {
+    m->wn[l] = wn[l];
+    m->wk[l] = wk[l];
+    nf += (size_t)7 * wn[l] * wk[l] + 5 * wn[l];  // w gw mw vw maskw + b gb mb vb
+    nb += (size_t)wn[l] * wk[l];
+  }
+  const size_t B = (size_t)batch_max;
+  nf += 4 * B * H + B * H * 2 + B * 3 * 2 + B * RH_MLP_IN + B;  // Z0-2, Z3(8), dA, dZf, y, target, xin, loss
+  nb += B * KIN + 3 * B * H + 3 * B * H + B * NOUT;              // X0, A0-2, dZb0-2, dZb3
+  int r = RH_OK;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreate(&m->st) != cudaSuccess ||
+      cudaMalloc(&m->P, nf * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&m->Pb, nb * sizeof(__nv_bfloat16)) != cudaSuccess) {
+    m->err = "allocation failed";
+    r = RH_ERR_NOMEM;
+  }
+  if (r == RH_OK) {
+    cudaMemset(m->P, 0, nf * sizeof(float));
+    cudaMemset(m->Pb, 0, nb * sizeof(__nv_bfloat16));
+    float* p = m->P;
+    __nv_bfloat16* pb = m->Pb;
+    for (int l = 0; l < 4; ++l) {
+      const size_t nw = (size_t)wn[l] * wk[l];
+      m->w[l] = p; p += nw;
+      m->gw[l] = p; p += nw;
+      m->mw[l] = p; p += nw;
+      m->vw[l] = p; p += nw;
+      m->maskw[l] = p; p += nw;
+      m->b[l] = p; p += wn[l];
+      m->gb[l] = p; p += wn[l];
+      m->mb[l] = p; p += wn[l];
+      m->vb[l] = p; p += wn[l];
+      p += (size_t)2 * nw;  // spare (keeps the arithmetic above honest)
+      p += wn[l];
+      m->wb[l] = pb; pb += nw;
+    }
+    m->Z[0] = p; p += B * H;
+    m->Z[1] = p; p += B * H;
+    m->Z[2] = p; p += B * H;
+    m->Z[3] = p; p += B * H;  // only B*NOUT used
+    m->dA = p; p += B * H;
+    m->dZf = p; p += B * H;
+    m->y = p; p += B * 3;
+    m->target = p; p += B * 3;
+    m->xin = p; p += B * RH_MLP_IN;
+    m->loss = p; p += B;
+    m->X0 = pb; pb += B * KIN;
+    for (int l = 0; l < 3; ++l) { m->A[l] = pb; pb += B * H; }
+    for (int l = 0; l < 3; ++l) { m->dZb[l] = pb; pb += B * H; }
+    m->dZb[3] = pb; pb += B * NOUT;
+    // masks: real weights 1, padding 0 (layer 1 inputs >= 4, layer 4 outputs >= 3)
+    for (int l = 0; l < 4; ++l) {
+      std::vector<float> mk((size_t)wn[l] * wk[l], 1.f);
+      for (int n = 0; n < wn[l]; ++n)
+        for (int k = 0; k < wk[l]; ++k)
+          if ((l == 0 && k >= RH_MLP_IN) || (l == 3 && n >= RH_MLP_OUT)) mk[(size_t)n * wk[l] + k] = 0.f;
+      cudaMemcpy(m->maskw[l], mk.data(), mk.size() * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+      m->err = "initialisation failed";
+      r = RH_ERR_CUDA;
+    }
+  }
+  if (r != RH_OK) {
+    rh_mlp_destroy(m);
+    return r;
+  }
+  *out = m;
+  return RH_OK;
+}
+
+int rh_mlp_destroy(rh_mlp* m) {
+  if (!m) return RH_ERR_ARG;
+  if (m->st) cudaStreamSynchronize(m->st);
+  cudaFree(m->P);
+  cudaFree(m->Pb);
+  if (m->st) cudaStreamDestroy(m->st);
+  delete m;
+  return RH_OK;
+}
+
+int rh_mlp_param_count(const rh_mlp* m, int32_t* n) {
+  if (!m || !n) return RH_ERR_ARG;
+  int s = 0;
+  for (int l = 0; l < 4; ++l) s += m->wn[l] * m->wk[l] + m->wn[l];
+  *n = s;
+  return RH_OK;
+}
+
+// Parameter order: for each layer, W (n x k row-major, padded) then b (n).
+int rh_mlp_set_params(rh_mlp* m, const float* params) {
+  if (!m || !params) return RH_ERR_ARG;
+  const float* p = params;
+  for (int l = 0; l < 4; ++l) {
+    const size_t nw = (size_t)m->wn[l] * m->wk[l];
+    MCK(cudaMemcpy(m->w[l], p, nw * sizeof(float), cudaMemcpyHostToDevice));
+    p += nw;
+    MCK(cudaMemcpy(m->b[l], p, m->wn[l] * sizeof(float), cudaMemcpyHostToDevice));
+    p += m->wn[l];
+    // apply the padding mask and refresh BF16 copies; reset Adam
+    adam_update<<<blocks(nw, 256), 256, 0, m->st>>>(m->w[l], m->gw[l], m->mw[l], m->vw[l], m->wb[l],
+                                                   m->maskw[l], (int)nw, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
+    MCK(cudaMemsetAsync(m->mw[l], 0, nw * sizeof(float), m->st));
+    MCK(cudaMemsetAsync(m->vw[l], 0, nw * sizeof(float), m->st));
+    MCK(cudaMemsetAsync(m->mb[l], 0, m->wn[l] * sizeof(float), m->st));
+    MCK(cudaMemsetAsync(m->vb[l], 0, m->wn[l] * sizeof(float), m->st));
+  }
+  m->step = 0;
+  MCK(cudaStreamSynchronize(m->st));
+  return RH_OK;
+}
+
+int rh_mlp_get_params(rh_mlp* m, float* params) {
+  if (!m || !params) return RH_ERR_ARG;
+  MCK(cudaStreamSynchronize(m->st));
+  float* p = params;
+  for (int l = 0; l < 4; ++l) {
+    const size_t nw = (size_t)m->wn[l] * m->wk[l];
+    MCK(cudaMemcpy(p, m->w[l], nw * sizeof(float), cudaMemcpyDeviceToHost));
+    p += nw;
+    MCK(cudaMemcpy(p, m->b[l], m->wn[l] * sizeof(float), cudaMemcpyDeviceToHost));
+    p += m->wn[l];
+  }
+  return RH_OK;
+}
+
+int rh_mlp_forward(rh_mlp* m, const float* x, int32_t n, float* y) {
+  if (!m || !x || !y || n <= 0) return RH_ERR_ARG;
+  for (int32_t off = 0; off < n; off += m->bmax) {
+    const int B = (int)std::min<int64_t>(m->bmax, n - off);
+    int r = run_loss(m, B, x + (size_t)off * RH_MLP_IN, nullptr, nullptr);
+    if (r) return r;
+    MCK(cudaMemcpyAsync(y + (size_t)off * 3, m->y, sizeof(float) * 3 * B, cudaMemcpyDeviceToHost,
+                        m->st));
+  }
+  MCK(cudaStreamSynchronize(m->st));
+  return RH_OK;
+}
+
+int rh_mlp_gradients(rh_mlp* m, const float* x, const float* target, int32_t n, float* grads,
+                     float* loss) {
+  if (!m || !x || !target || n <= 0 || n > m->bmax) return RH_ERR_ARG;
+  int r = run_loss(m, n, x, target, loss);
+  if (r) return r;
+  if ((r = backward(m, n))) return r;
+  if (grads) {
+    MCK(cudaStreamSynchronize(m->st));
+    float* p = grads;
+    for (int l = 0; l < 4; ++l) {
+      const size_t nw = (size_t)m->wn[l] * m->wk[l];
+      MCK(cudaMemcpy(p, m->gw[l], nw * sizeof(float), cudaMemcpyDeviceToHost));
+      p += nw;
+      MCK(cudaMemcpy(p, m->gb[l], m->wn[l] * sizeof(float), cudaMemcpyDeviceToHost));
+      p += m->wn[l];
+    }
+  }
+  return RH_OK;
+}
+
+int rh_mlp_train_step(rh_mlp* m, const float* x, const float* target, int32_t n, float lr,
+                      float* loss) {
+  int r = rh_mlp_gradients(m, x, target, n, nullptr, loss);
+  if (r) return r;
+  m->step += 1;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float bc1 = 1.f - powf(b1, (float)m->step), bc2 = 1.f - powf(b2, (float)m->step);
+  for (int l = 0; l < 4; ++l) {
+    const int nw = m->wn[l] * m->wk[l];
+    adam_update<<<blocks(nw, 256), 256, 0, m->st>>>(m->w[l], m->gw[l], m->mw[l], m->vw[l], m->wb[l],
+                                                   m->maskw[l], nw, lr, b1, b2, eps, bc1, bc2);
+    adam_update<<<blocks(m->wn[l], 128), 128, 0, m->st>>>(m->b[l], m->gb[l], m->mb[l], m->vb[l],
+                                                         nullptr, nullptr, m->wn[l], lr, b1, b2, eps,
+                                                         bc1, bc2);
+  }
+  MCK(cudaGetLastError());
+  MCK(cudaStreamSynchronize(m->st));
+  return RH_OK;
+}
+
+int rh_mlp_last_error(const rh_mlp* m, char* buf, size_t n) {
+  if (!buf || n == 0) return RH_ERR_ARG;
+  snprintf(buf, n, "%s", m ? m->err.c_str() : "");
+  return RH_OK;
+}
+
+}  // extern "C"

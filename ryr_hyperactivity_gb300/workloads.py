@@ -1,7 +1,7 @@
 """Synthetic workloads (no dataset is involved: every input is a seeded set of
 cell parameters).  Parameter bases follow run.sh:7-9: "stab" uses a6 = 10,
-a8 = 1.0; the other arguments are a3 = 1.0, a4 = 740, a5 = 1.0, a7 = 0,
-a9 = 0.7, a10 = 1."""
+a8 = 1.0, "hyper" a6 = 3.333, a8 = 18; the other arguments are a3 = 1.0,
+a4 = 740, a5 = 1.0, a7 = 0, a9 = 0.7, a10 = 1."""
 from __future__ import annotations
 
 import numpy as np
@@ -10,6 +10,7 @@ from .abi import CellParams, cell_params
 
 STAB = dict(clamp_mv=1.0, cjsr_basal=740.0, ncx_scale=1.0, ku=10.0, r1=0.0, kb=1.0,
             ica_scale=0.7, ku2=1.0)
+HYPER = dict(STAB, ku=3.333, kb=18.0)
 
 
 def config1_cell(seed: int = 1) -> CellParams:
@@ -31,7 +32,8 @@ def config3_cells(n: int = 512, param_seed: int = 12345, philox_seed: int = 1,
                   first_id: int = 0, nbeats: int = 20) -> list[CellParams]:
     """Heterogeneous ensemble: nx~U{60..100}, ny~U{12..20}, nz~U{6..10},
     RyR open-rate scale Ku2~U[1,3], IKr scale~U[0,1], PCL~U[500,3000] ms;
-    iso2 build with IKr scaled (lqt off); Philox key = (seed, cell id)."""
+    the RyR-hyperactive parameter base of run.sh:9, iso2 build with IKr
+    scaled (lqt off); Philox key = (seed, cell id)."""
     rng = np.random.default_rng(param_seed)
     nx = rng.integers(60, 101, n)
     ny = rng.integers(12, 21, n)
@@ -41,7 +43,7 @@ def config3_cells(n: int = 512, param_seed: int = 12345, philox_seed: int = 1,
     pcl = rng.uniform(500.0, 3000.0, n)
     cells = []
     for c in range(n):
-        d = dict(STAB)
+        d = dict(HYPER)
         d["ku2"] = float(ku2[c])
         cells.append(cell_params(nx=int(nx[c]), ny=int(ny[c]), nz=int(nz[c]), nbeats=nbeats,
                                  pcl_ms=float(pcl[c]), lqt=0, iso2=1, ikr_scale=float(ikr[c]),
