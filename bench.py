@@ -197,6 +197,7 @@ def main():
     bpc = sim.bytes_per_cru_step()
     for _ in range(args.warmup):
         sim.run_steps(WINDOW)
+    tile, tune_ms = sim.autotune(40)  # CRU-tile length for this workload (state unchanged)
     sim.kernel_timing()  # reset
     for c in range(sim.ncells):
         sim.drain_wholecell(c)
@@ -235,7 +236,9 @@ def main():
                    "cells": args.cells, "interior_crus": n_in, "window_steps": WINDOW,
                    "step": "one output window = 100 lattice updates of every cell",
                    "l2": f"state {sim.state_bytes() / 1e9:.2f} GB > 129 MB L2, no flush",
-                   "parallelism": f"cells sharded, {world} GPU(s)"},
+                   "parallelism": f"cells sharded, {world} GPU(s)",
+                   "tile_crus": tile,
+                   "autotune_ms_per_step": {str(t): round(m, 4) for t, m in zip((64, 128, 256), tune_ms)}},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if peak else None, "traffic": traffic,

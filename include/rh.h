@@ -98,7 +98,7 @@ typedef struct {
   int32_t precision;          /* RH_FP64 or RH_MIXED */
   int32_t device;             /* CUDA device ordinal */
   double dt_ms;               /* time step (reference DT 0.025, :51) */
-  int32_t block_size;         /* CRUs per CTA; 0 = use the tuned default */
+  int32_t block_size;         /* CRUs per CTA (64, 128 or 256); 0 = 128 */
   int32_t output_capacity;    /* wholecell records kept per cell between drains */
   int32_t record_linescan;    /* 1 = keep linescan rows at output steps */
   int32_t track_stats;        /* 1 = per-beat APD90/EAD/peak-ci/SR-load/sparks */
@@ -219,6 +219,15 @@ int rh_restore(rh_sim* sim, const char* path);
 int rh_state_bytes(const rh_sim* sim, size_t* bytes);
 int rh_export_state(rh_sim* sim, void* host, size_t bytes);
 int rh_import_state(rh_sim* sim, const void* host, size_t bytes);
+
+/* CRU-tile autotuner.  The step kernel is compiled for tiles of 64, 128 and
+ * 256 CRUs per CTA (each with its own register/occupancy bound).  Times
+ * `steps` lattice updates of the live workload with each candidate, starting
+ * every candidate from a device-side copy of the current state and restoring
+ * that state afterwards (the simulation does not advance), then keeps the
+ * fastest.  ms_per_step (3 entries, may be NULL) receives the timings. */
+int rh_autotune(rh_sim* sim, int32_t steps, int32_t* tile_crus, double* ms_per_step);
+int rh_tile_size(const rh_sim* sim, int32_t* tile_crus);
 
 /* Algorithmic HBM bytes moved per interior CRU per lattice update for the
  * simulator's precision (each persistent field read once, written once). */

@@ -26,9 +26,17 @@ struct rh_sim {
   int ncells = 0;
   rh_run_opts opts{};
   std::vector<rh_cell_params> params;
-  std::vector<CellConst> hcells;
-  std::vector<int4> htiles;
-  int ntiles = 0;
+  std::vector<CellConst> hcells;  // per-cell constants (tile fields of the current set)
+  // one tile table per compiled tile length (kTileSizes); `ts` is in use
+  struct TileSet {
+    int tile = 0;
+    int ntiles = 0;
+    std::vector<CellConst> hcells;
+    std::vector<int4> htiles;
+    CellConst* d_cells = nullptr;
+    int4* d_tiles = nullptr;
+  } sets[kNumTileSizes];
+  int ts = 0;
   int64_t stride = 0;
   int max_n = 0;
   int device = 0;
@@ -38,9 +46,7 @@ struct rh_sim {
   size_t arena_bytes = 0;
   Lattice<double> Ld{};
   Lattice<float> Lf{};
-  CellConst* d_cells = nullptr;
   CellDyn* d_dyn = nullptr;
-  int4* d_tiles = nullptr;
   double* d_partials = nullptr;
   double* d_out_wc = nullptr;
   double* d_out_ls = nullptr;
@@ -195,9 +201,9 @@ template <class R>
 StepArgs<R> make_args(rh_sim* s, const Lattice<R>& L, bool lattice_only) {
   StepArgs<R> a{};
   a.L = L;
-  a.cells = s->d_cells;
+  a.cells = s->sets[s->ts].d_cells;
   a.dyn = s->d_dyn;
-  a.tiles = s->d_tiles;
+  a.tiles = s->sets[s->ts].d_tiles;
   a.partials = s->d_partials;
   a.out_wc = s->d_out_wc;
   a.out_ls = s->d_out_ls;
@@ -211,8 +217,10 @@ StepArgs<R> make_args(rh_sim* s, const Lattice<R>& L, bool lattice_only) {
 }
 
 cudaError_t launch_one(rh_sim* s, bool out, bool lattice_only) {
-  if (is_mixed(s)) return launch_step<float>(make_args(s, s->Lf, lattice_only), s->ntiles, out, s->stream);
-  return launch_step<double>(make_args(s, s->Ld, lattice_only), s->ntiles, out, s->stream);
+  const rh_sim::TileSet& t = s->sets[s->ts];
+  if (is_mixed(s))
+    return launch_step<float>(make_args(s, s->Lf, lattice_only), t.ntiles, out, t.tile, s->stream);
+  return launch_step<double>(make_args(s, s->Ld, lattice_only), t.ntiles, out, t.tile, s->stream);
 }
 
 bool out_step_host(double t, double dt) { return fmod(t + 0.0000001, OUTT) < dt; }
@@ -373,9 +381,6 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     cc.nyf = p.ny;
     cc.n = (int)n64;
     cc.off = off;
-    cc.tile_begin = tiles;
-    const int kb = s->opts.precision == RH_MIXED ? block_of<float>() : block_of<double>();
-    cc.tile_count = (cc.n + kb - 1) / kb;
     int jz = p.linescan_jz < 0 ? 5 : p.linescan_jz;
     if (jz > p.nz - 2) jz = p.nz / 2;
     if (jz < 1) jz = 1;
@@ -399,15 +404,37 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     cc.kb = p.kb;
     cc.pcl = p.pcl_ms;
     cc.tend = p.nbeats * p.pcl_ms + 2100;
-    for (int t = 0; t < cc.tile_count; ++t)
-      s->htiles.push_back(make_int4(c, t * kb, std::min(kb, cc.n - t * kb), 0));
-    tiles += cc.tile_count;
     off += (n64 + 31) & ~int64_t(31);
     ls_off += (int64_t)s->opts.output_capacity * cc.lx;
     s->max_n = std::max(s->max_n, cc.n);
     s->hcells.push_back(cc);
   }
-  s->ntiles = tiles;
+  int max_tiles = 0;
+  for (int k = 0; k < kNumTileSizes; ++k) {
+    rh_sim::TileSet& t = s->sets[k];
+    t.tile = kTileSizes[k];
+    t.hcells = s->hcells;
+    int nt = 0;
+    for (int c = 0; c < ncells; ++c) {
+      CellConst& cc = t.hcells[c];
+      cc.tile_begin = nt;
+      cc.tile_count = (cc.n + t.tile - 1) / t.tile;
+      for (int q = 0; q < cc.tile_count; ++q)
+        t.htiles.push_back(make_int4(c, q * t.tile, std::min(t.tile, cc.n - q * t.tile), 0));
+      nt += cc.tile_count;
+    }
+    t.ntiles = nt;
+    max_tiles = std::max(max_tiles, nt);
+  }
+  {
+    int want = s->opts.block_size > 0 ? s->opts.block_size : kDefaultTile;
+    s->ts = -1;
+    for (int k = 0; k < kNumTileSizes; ++k)
+      if (kTileSizes[k] == want) s->ts = k;
+    if (s->ts < 0) return fail(s, RH_ERR_ARG, "block_size %d is not a compiled tile length", want);
+  }
+  s->hcells = s->sets[s->ts].hcells;
+  (void)tiles;
   s->stride = off;
   s->ls_rows_total = ls_off;
   s->device = s->opts.device;
@@ -424,19 +451,22 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   char* p = reinterpret_cast<char*>(s->arena);
   if (is_mixed(s)) carve(s->Lf, p, s->stride);
   else carve(s->Ld, p, s->stride);
-  CK(cudaMalloc(&s->d_cells, sizeof(CellConst) * ncells));
   CK(cudaMalloc(&s->d_dyn, sizeof(CellDyn) * ncells));
-  CK(cudaMalloc(&s->d_tiles, sizeof(int4) * tiles));
-  CK(cudaMalloc(&s->d_partials, sizeof(double) * P_COUNT * (size_t)tiles));
+  for (int k = 0; k < kNumTileSizes; ++k) {
+    rh_sim::TileSet& t = s->sets[k];
+    CK(cudaMalloc(&t.d_cells, sizeof(CellConst) * ncells));
+    CK(cudaMalloc(&t.d_tiles, sizeof(int4) * t.ntiles));
+    CK(cudaMemcpyAsync(t.d_cells, t.hcells.data(), sizeof(CellConst) * ncells,
+                       cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(t.d_tiles, t.htiles.data(), sizeof(int4) * t.ntiles,
+                       cudaMemcpyHostToDevice, s->stream));
+  }
+  CK(cudaMalloc(&s->d_partials, sizeof(double) * P_COUNT * (size_t)max_tiles));
   CK(cudaMalloc(&s->d_out_wc, sizeof(double) * RH_WHOLECELL_COLS * (size_t)ncells *
                                   s->opts.output_capacity));
   CK(cudaMalloc(&s->d_out_ls, sizeof(double) * RH_LINESCAN_COLS * (size_t)std::max<int64_t>(ls_off, 1)));
   if (s->opts.track_stats)
     CK(cudaMalloc(&s->d_stats, sizeof(rh_beat_stats) * (size_t)ncells * s->opts.stats_capacity));
-  CK(cudaMemcpyAsync(s->d_cells, s->hcells.data(), sizeof(CellConst) * ncells,
-                     cudaMemcpyHostToDevice, s->stream));
-  CK(cudaMemcpyAsync(s->d_tiles, s->htiles.data(), sizeof(int4) * tiles, cudaMemcpyHostToDevice,
-                     s->stream));
   // cells' basal state and membrane initial conditions
   std::vector<InitValues> iv(ncells);
   std::vector<CellDyn> dyn(ncells);
@@ -457,9 +487,10 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   CK(cudaMalloc(&d_iv, sizeof(InitValues) * ncells));
   CK(cudaMemcpyAsync(d_iv, iv.data(), sizeof(InitValues) * ncells, cudaMemcpyHostToDevice, s->stream));
   CK(cudaMemcpyAsync(s->d_dyn, dyn.data(), sizeof(CellDyn) * ncells, cudaMemcpyHostToDevice, s->stream));
-  if (is_mixed(s)) CK(launch_init<float>(s->Lf, s->d_cells, d_iv, ncells, s->max_n, s->stream));
-  else CK(launch_init<double>(s->Ld, s->d_cells, d_iv, ncells, s->max_n, s->stream));
-  CK(launch_volt_prep(s->d_cells, s->d_dyn, ncells, s->opts.dt_ms, s->stream));
+  const CellConst* dcells = s->sets[s->ts].d_cells;
+  if (is_mixed(s)) CK(launch_init<float>(s->Lf, dcells, d_iv, ncells, s->max_n, s->stream));
+  else CK(launch_init<double>(s->Ld, dcells, d_iv, ncells, s->max_n, s->stream));
+  CK(launch_volt_prep(dcells, s->d_dyn, ncells, s->opts.dt_ms, s->stream));
   if (s->opts.keep_diagnostics) {
     int r = ensure_diag(s);
     if (r) return r;
@@ -477,9 +508,11 @@ int rh_destroy(rh_sim* s) {
   }
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   cudaFree(s->arena);
-  cudaFree(s->d_cells);
+  for (auto& t : s->sets) {
+    cudaFree(t.d_cells);
+    cudaFree(t.d_tiles);
+  }
   cudaFree(s->d_dyn);
-  cudaFree(s->d_tiles);
   cudaFree(s->d_partials);
   cudaFree(s->d_out_wc);
   cudaFree(s->d_out_ls);
@@ -780,7 +813,7 @@ int rh_set_membrane(rh_sim* s, int32_t cell, const rh_membrane* src) {
   CK(cudaSetDevice(s->device));
   CK(cudaStreamSynchronize(s->stream));
   CK(cudaMemcpy(&s->d_dyn[cell].m, src, sizeof(rh_membrane), cudaMemcpyHostToDevice));
-  CK(launch_volt_prep(s->d_cells, s->d_dyn, s->ncells, s->opts.dt_ms, s->stream));
+  CK(launch_volt_prep(s->sets[s->ts].d_cells, s->d_dyn, s->ncells, s->opts.dt_ms, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   s->t_host[cell] = src->t;
   s->active_host[cell] = src->t < s->hcells[cell].tend;
@@ -1005,6 +1038,85 @@ int rh_import_state(rh_sim* s, const void* host, size_t bytes) {
   }
   CK(cudaStreamSynchronize(s->stream));
   return RH_OK;
+}
+
+int rh_tile_size(const rh_sim* s, int32_t* tile) {
+  if (!s || !tile) return RH_ERR_ARG;
+  *tile = s->sets[s->ts].tile;
+  return RH_OK;
+}
+
+int rh_autotune(rh_sim* s, int32_t steps, int32_t* tile, double* ms_per_step) {
+  if (!s || steps <= 0) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  // save the state on the device; every candidate starts from it
+  const size_t dyn_bytes = sizeof(CellDyn) * (size_t)s->ncells;
+  void* backup = nullptr;
+  if (cudaMalloc(&backup, s->arena_bytes + dyn_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(s, RH_ERR_NOMEM, "autotune: no room for a state copy");
+  }
+  char* bk = reinterpret_cast<char*>(backup);
+  CK(cudaMemcpyAsync(bk, s->arena, s->arena_bytes, cudaMemcpyDeviceToDevice, s->stream));
+  CK(cudaMemcpyAsync(bk + s->arena_bytes, s->d_dyn, dyn_bytes, cudaMemcpyDeviceToDevice, s->stream));
+  const std::vector<double> t0 = s->t_host;
+  const std::vector<char> a0 = s->active_host;
+  const int ts0 = s->ts;
+  const double dt = s->opts.dt_ms;
+  double best = 1e300;
+  int best_k = ts0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int rc = RH_OK;
+  for (int k = 0; k < kNumTileSizes && rc == RH_OK; ++k) {
+    s->ts = k;
+    cudaMemcpyAsync(s->arena, bk, s->arena_bytes, cudaMemcpyDeviceToDevice, s->stream);
+    cudaMemcpyAsync(s->d_dyn, bk + s->arena_bytes, dyn_bytes, cudaMemcpyDeviceToDevice, s->stream);
+    std::vector<double> th = t0;
+    cudaEventRecord(e0, s->stream);
+    for (int i = 0; i < steps; ++i) {
+      bool out = false;
+      for (int c = 0; c < s->ncells; ++c)
+        if (a0[c] && out_step_host(th[c], dt)) out = true;
+      for (int c = 0; c < s->ncells; ++c) th[c] = th[c] + dt;
+      cudaError_t e = launch_one(s, out, false);
+      if (e != cudaSuccess) {
+        rc = fail(s, RH_ERR_CUDA, "autotune launch: %s", cudaGetErrorString(e));
+        break;
+      }
+    }
+    cudaEventRecord(e1, s->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = fail(s, RH_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    double per = ms / steps;
+    if (ms_per_step) ms_per_step[k] = per;
+    if (per < best) {
+      best = per;
+      best_k = k;
+    }
+  }
+  // restore the state and select the winner
+  cudaMemcpyAsync(s->arena, bk, s->arena_bytes, cudaMemcpyDeviceToDevice, s->stream);
+  cudaMemcpyAsync(s->d_dyn, bk + s->arena_bytes, dyn_bytes, cudaMemcpyDeviceToDevice, s->stream);
+  cudaStreamSynchronize(s->stream);
+  cudaFree(backup);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->t_host = t0;
+  s->active_host = a0;
+  s->ts = rc == RH_OK ? best_k : ts0;
+  s->hcells = s->sets[s->ts].hcells;
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+  if (tile) *tile = s->sets[s->ts].tile;
+  CK(cudaGetLastError());
+  return rc;
 }
 
 int rh_bytes_per_cru_step(const rh_sim* s, double* bytes) {

@@ -1,7 +1,7 @@
 // step.cu — the fused per-time-step kernel.
 //
 // One launch advances every active cell by one time step:
-//   1. each CTA owns a tile of up to kBlock consecutive CRUs of one cell and
+//   1. each CTA owns a tile of up to B consecutive CRUs of one cell and
 //      updates them as the reference's Compute kernel does
 //      (cuda_Cell_Detailed.cu:1187-1692, fixA): the tile's own ci/cnsr
 //      sub-voxels are staged in shared memory so that in-tile stencil
@@ -180,9 +180,9 @@ struct TileHeader {
   int parity, done;
 };
 
-template <class R, bool OUT>
-__global__ void __launch_bounds__(block_of<R>(), min_blocks<R>()) step_kernel(StepArgs<R> a) {
-  constexpr int kBlock = block_of<R>();
+template <class R, bool OUT, int B>
+__global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArgs<R> a) {
+  constexpr int kBlock = B;
   __shared__ TileHeader sh;
   __shared__ StepCoef<R> sk;
   using V = typename Vec2<R>::T;
@@ -832,13 +832,23 @@ __global__ void coef_prep_kernel(const CellConst* cells, CellDyn* dyn, int ncell
 
 // ------------------------------------------------------------- launchers
 
-template <class R>
-cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, cudaStream_t st) {
-  if (ntiles <= 0) return cudaSuccess;
+template <class R, int B>
+void launch_b(const StepArgs<R>& a, int ntiles, bool out, cudaStream_t st) {
   if (out)
-    step_kernel<R, true><<<ntiles, block_of<R>(), 0, st>>>(a);
+    step_kernel<R, true, B><<<ntiles, B, 0, st>>>(a);
   else
-    step_kernel<R, false><<<ntiles, block_of<R>(), 0, st>>>(a);
+    step_kernel<R, false, B><<<ntiles, B, 0, st>>>(a);
+}
+
+template <class R>
+cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, int tile, cudaStream_t st) {
+  if (ntiles <= 0) return cudaSuccess;
+  switch (tile) {
+    case 64: launch_b<R, 64>(a, ntiles, out, st); break;
+    case 128: launch_b<R, 128>(a, ntiles, out, st); break;
+    case 256: launch_b<R, 256>(a, ntiles, out, st); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
@@ -857,8 +867,8 @@ cudaError_t launch_volt_prep(const CellConst* cells, CellDyn* dyn, int ncells, d
   return cudaGetLastError();
 }
 
-template cudaError_t launch_step<double>(const StepArgs<double>&, int, bool, cudaStream_t);
-template cudaError_t launch_step<float>(const StepArgs<float>&, int, bool, cudaStream_t);
+template cudaError_t launch_step<double>(const StepArgs<double>&, int, bool, int, cudaStream_t);
+template cudaError_t launch_step<float>(const StepArgs<float>&, int, bool, int, cudaStream_t);
 template cudaError_t launch_init<double>(const Lattice<double>&, const CellConst*,
                                          const InitValues*, int, int, cudaStream_t);
 template cudaError_t launch_init<float>(const Lattice<float>&, const CellConst*,

@@ -7,19 +7,20 @@
 
 namespace rh {
 
-// CRUs (threads) per CTA of the step kernel.
-template <class R>
-__host__ __device__ constexpr int block_of() {
-  return 128;
-}
+// Tile lengths (CRUs = threads per CTA) the step kernel is compiled for; the
+// autotuner (rh_autotune) picks one per simulator.
+constexpr int kNumTileSizes = 3;
+constexpr int kTileSizes[kNumTileSizes] = {64, 128, 256};
+constexpr int kDefaultTile = 128;
 
-// Resident CTAs per SM the register allocation is bounded for: the FP32
-// kernel is latency-bound and wants warps (5 x 128 threads at <= 102
-// registers measured best); the FP64 kernel is bound by the FP64 pipe and
-// wants registers.
-template <class R>
-__host__ __device__ constexpr int min_blocks() {
-  return sizeof(R) == 4 ? 5 : 3;
+// Resident CTAs per SM each instantiation's register allocation is bounded
+// for.  FP32: about 640 threads per SM at <= ~100 registers (measured best:
+// the kernel is latency-bound and wants warps).  FP64: bound by the FP64 pipe,
+// so fewer, register-rich threads.
+template <class R, int B>
+__host__ __device__ constexpr int min_blocks_for() {
+  return sizeof(R) == 4 ? (B == 64 ? 10 : (B == 128 ? 5 : 2))
+                        : (B == 64 ? 6 : (B == 128 ? 3 : 1));
 }
 
 // Basal values of one cell (Init kernel, cuda_Cell_Detailed.cu:1121-1174),
@@ -31,8 +32,9 @@ struct InitValues {
   uint32_t lcc_lo, lcc_hi;
 };
 
+// One time step with tiles of `tile` CRUs (one of kTileSizes).
 template <class R>
-cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, cudaStream_t st);
+cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, int tile, cudaStream_t st);
 
 template <class R>
 cudaError_t launch_init(const Lattice<R>& L, const CellConst* cells, const InitValues* iv,

@@ -20,7 +20,7 @@ EXPORTS = [
     "rh_drain_linescan", "rh_drain_stats", "rh_cell_status", "rh_checkpoint", "rh_restore",
     "rh_bytes_per_cru_step", "rh_kernel_timing", "rh_last_error", "rh_format_wholecell",
     "rh_format_linescan", "rh_state_bytes", "rh_export_state", "rh_import_state",
-    "rh_analyze_trace",
+    "rh_analyze_trace", "rh_autotune", "rh_tile_size",
 ]
 
 _lib = None
@@ -68,6 +68,8 @@ def load() -> C.CDLL:
     L.rh_export_state.argtypes = [vp, vp, C.c_size_t]
     L.rh_import_state.argtypes = [vp, vp, C.c_size_t]
     L.rh_kernel_timing.argtypes = [vp, C.POINTER(C.c_int64), dp]
+    L.rh_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), dp]
+    L.rh_tile_size.argtypes = [vp, C.POINTER(C.c_int32)]
     L.rh_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
     L.rh_format_wholecell.argtypes = [dp, C.c_char_p, C.c_size_t]
     L.rh_format_linescan.argtypes = [dp, C.c_char_p, C.c_size_t]

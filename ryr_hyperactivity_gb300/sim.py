@@ -147,6 +147,19 @@ class Simulator:
     def import_state(self, ptr: int, nbytes: int) -> None:
         self._ck(self.L.rh_import_state(self.h, C.c_void_p(ptr), nbytes))
 
+    def autotune(self, steps: int = 50) -> tuple[int, list[float]]:
+        """Picks the fastest tile length for this workload; returns it and the
+        measured ms per step of each candidate (64, 128, 256 CRUs)."""
+        tile = C.c_int32()
+        ms = (C.c_double * 3)()
+        self._ck(self.L.rh_autotune(self.h, int(steps), C.byref(tile), ms))
+        return tile.value, list(ms)
+
+    def tile_size(self) -> int:
+        t = C.c_int32()
+        self._ck(self.L.rh_tile_size(self.h, C.byref(t)))
+        return t.value
+
     def bytes_per_cru_step(self) -> float:
         b = C.c_double()
         self._ck(self.L.rh_bytes_per_cru_step(self.h, C.byref(b)))

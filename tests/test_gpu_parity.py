@@ -209,3 +209,34 @@ def test_cli_dropin_matches_oracle_files():
         va = np.array([float(x) for x in fa if x]), np.array([float(x) for x in fb if x])
         np.testing.assert_allclose(va[0], va[1], rtol=1e-5, atol=2e-6)
     assert len(lst.splitlines()) == len(want_ls.splitlines())
+
+
+def test_tile_sizes_agree_and_autotune_leaves_state_unchanged():
+    cells = [c1_params(nx=30, ny=12, nz=6, seed=2, cell_id=0),
+             c1_params(nx=17, ny=9, nz=5, seed=2, cell_id=1, ku2=2.0)]
+    ref = None
+    for tile in (64, 128, 256):
+        with Simulator(cells, precision="fp64", block_size=tile) as sim:
+            assert sim.tile_size() == tile
+            sim.run_steps(600)
+            st = [sim.get_state(c).snapshot() for c in range(2)]
+            mv = [sim.get_membrane(c).v for c in range(2)]
+        if ref is None:
+            ref = (st, mv)
+            continue
+        for c in range(2):
+            for k in ("nou", "ncu", "nob", "ncb", "lcc"):
+                np.testing.assert_array_equal(st[c][k], ref[0][c][k])
+            np.testing.assert_allclose(st[c]["ci"], ref[0][c]["ci"], rtol=1e-12)
+            assert abs(mv[c] - ref[1][c]) < 1e-10
+    with Simulator(cells, precision="mixed") as a, Simulator(cells, precision="mixed") as b:
+        a.run_steps(300)
+        b.run_steps(300)
+        tile, ms = a.autotune(20)
+        assert tile in (64, 128, 256) and all(m > 0 for m in ms)
+        assert a.get_membrane(0).step == b.get_membrane(0).step == 300
+        a.run_steps(200)
+        b.run_steps(200)
+        for c in range(2):
+            for k in ("nou", "ncb", "lcc"):
+                np.testing.assert_array_equal(a.get_state(c)[k], b.get_state(c)[k])
