@@ -47,6 +47,34 @@ int rh_mlp_train_step(rh_mlp* m, const float* x, const float* target, int32_t n,
                       float* loss);
 int rh_mlp_last_error(const rh_mlp* m, char* buf, size_t n);
 
+/* Forward pass that allocates nothing.  It has no counterpart in the
+ * reference.  It is for callers that may not call cudaMalloc themselves or
+ * have the library call it: programs whose device memory belongs to their own
+ * allocator or pool, and loops that cannot take the synchronisation an
+ * allocation can bring.
+ *
+ * d_params: device FP32 parameter vector in the layout above (what
+ * rh_mlp_get_params returns); d_x: device [n x 4]; d_y: device [n x 3]; all
+ * on the calling thread's current device.  Same kernels and the same result
+ * as rh_mlp_forward with those parameters.  The work is queued on `stream`
+ * (a cudaStream_t; NULL = the default stream) and the call returns without
+ * waiting for it.
+ *
+ * The intermediate values live in one fixed device array inside the library,
+ * RH_MLP_NOALLOC_SCRATCH_BYTES (4 MiB) per device, held from the library's
+ * loading until process exit.  n above RH_MLP_NOALLOC_MAX_BATCH is rejected
+ * with RH_ERR_ARG and a message in err (err may be NULL).  The first call on
+ * a device looks up that array's device address (one-time set-up); make that
+ * first call before any stream capture.  All calls on a device share the
+ * array: two calls whose work overlaps on the GPU (different streams, or
+ * different threads without ordering) race and give wrong results.  Each
+ * call writes every scratch value it reads, so nothing left by an earlier
+ * call reaches the result. */
+#define RH_MLP_NOALLOC_MAX_BATCH 4096
+#define RH_MLP_NOALLOC_SCRATCH_BYTES (4 * 1024 * 1024)
+int rh_mlp_forward_noalloc(const float* d_params, const float* d_x, int32_t n, float* d_y,
+                           void* stream, char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,11 +12,13 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdarg.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -467,3 +469,164 @@ int rh_mlp_last_error(const rh_mlp* m, char* buf, size_t n) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ forward pass without allocation
+//
+// rh_mlp_forward above works on a handle whose buffers rh_mlp_create obtained
+// with cudaMalloc.  Some callers cannot make that call: a host program whose
+// device memory is all handed out by its own allocator or pool, a co-simulation
+// loop that budgets device memory up front, or a caller that must not pay the
+// device-wide synchronisation an allocation can imply.  rh_mlp_forward_noalloc
+// serves them: the caller brings the parameters, inputs and outputs in device
+// memory, and the intermediate values (BF16 weight copies, packed inputs,
+// pre-activations, activations, output-layer terms) live in the fixed array
+// below, which is part of the library image on every device that loads it.
+
+static __device__ __align__(256) unsigned char g_forward_scratch[RH_MLP_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+// Byte offsets inside the scratch array, each a multiple of 256.
+constexpr size_t kNaRows = RH_MLP_NOALLOC_MAX_BATCH;
+constexpr size_t kNaWeights = (size_t)H * KIN + 2 * (size_t)H * H + (size_t)NOUT * H;
+constexpr size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t kOffW = 0;
+constexpr size_t kOffX0 = kOffW + round256(kNaWeights * 2);
+constexpr size_t kOffZ = kOffX0 + round256(kNaRows * KIN * 2);
+constexpr size_t kOffA = kOffZ + round256(kNaRows * H * 4);
+constexpr size_t kOffDz = kOffA + round256(kNaRows * H * 2);
+constexpr size_t kOffDzb = kOffDz + round256(kNaRows * NOUT * 4);
+constexpr size_t kNaEnd = kOffDzb + round256(kNaRows * NOUT * 2);
+static_assert(kNaEnd <= RH_MLP_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the array");
+
+// FP32 weights of one layer -> BF16, padding entries (layer 1 inputs >= 4,
+// layer 4 outputs >= 3) forced to zero, as rh_mlp_set_params does.
+__global__ void weights_to_bf16(const float* w, __nv_bfloat16* wb, int n, int k, int nvalid,
+                                int kvalid) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * k) return;
+  const int r = i / k, c = i % k;
+  wb[i] = __float2bfloat16(r < nvalid && c < kvalid ? w[i] : 0.f);
+}
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_addr[kMaxDevices] = {};
+
+void na_msg(char* err, size_t len, const char* fmt, ...) __attribute__((format(printf, 3, 4)));
+void na_msg(char* err, size_t len, const char* fmt, ...) {
+  if (!err || len == 0) return;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(err, len, fmt, ap);
+  va_end(ap);
+}
+
+bool on_device(const void* p, int dev) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+extern "C" int rh_mlp_forward_noalloc(const float* d_params, const float* d_x, int32_t n,
+                                      float* d_y, void* stream, char* err, size_t err_len) {
+  if (err && err_len) err[0] = '\0';
+  if (!d_params || !d_x || !d_y) {
+    na_msg(err, err_len, "rh_mlp_forward_noalloc: params, x and y must be device pointers");
+    return RH_ERR_ARG;
+  }
+  if (n <= 0 || n > RH_MLP_NOALLOC_MAX_BATCH) {
+    na_msg(err, err_len,
+           "rh_mlp_forward_noalloc: n = %d is outside 1..%d, the largest batch its fixed "
+           "%d-byte scratch array holds; split the batch",
+           (int)n, RH_MLP_NOALLOC_MAX_BATCH, RH_MLP_NOALLOC_SCRATCH_BYTES);
+    return RH_ERR_ARG;
+  }
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    na_msg(err, err_len, "rh_mlp_forward_noalloc: no usable current device (%s)",
+           cudaGetErrorString(e));
+    return RH_ERR_CUDA;
+  }
+  if (!on_device(d_params, dev) || !on_device(d_x, dev) || !on_device(d_y, dev)) {
+    na_msg(err, err_len,
+           "rh_mlp_forward_noalloc: params, x and y must be device memory of the current "
+           "device %d",
+           dev);
+    return RH_ERR_ARG;
+  }
+  // Set-up, once per device, with that device current: the scratch array's
+  // device address.  Later calls reuse the cached address.
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_forward_scratch);
+      if (e != cudaSuccess || !p) {
+        na_msg(err, err_len, "rh_mlp_forward_noalloc: cudaGetSymbolAddress failed on device %d: %s",
+               dev, cudaGetErrorString(e));
+        return RH_ERR_CUDA;
+      }
+      g_scratch_addr[dev] = p;
+    }
+    base = g_scratch_addr[dev];
+  }
+  unsigned char* s = static_cast<unsigned char*>(base);
+  __nv_bfloat16* wb = reinterpret_cast<__nv_bfloat16*>(s + kOffW);
+  __nv_bfloat16* X0 = reinterpret_cast<__nv_bfloat16*>(s + kOffX0);
+  float* Z = reinterpret_cast<float*>(s + kOffZ);
+  __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(s + kOffA);
+  float* dz = reinterpret_cast<float*>(s + kOffDz);
+  __nv_bfloat16* dzb = reinterpret_cast<__nv_bfloat16*>(s + kOffDzb);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+  // Every scratch element read below is written earlier in this call, so the
+  // previous call's contents never leak into the result and nothing needs
+  // clearing.
+  const int wn[4] = {H, H, H, NOUT}, wk[4] = {KIN, H, H, H};
+  const float* wl[4];
+  const float* bl[4];
+  __nv_bfloat16* wbl[4];
+  {
+    const float* p = d_params;
+    __nv_bfloat16* q = wb;
+    for (int l = 0; l < 4; ++l) {
+      const int nw = wn[l] * wk[l];
+      wl[l] = p;
+      bl[l] = p + nw;
+      wbl[l] = q;
+      p += nw + wn[l];
+      q += nw;
+      weights_to_bf16<<<blocks(nw, 256), 256, 0, st>>>(wl[l], wbl[l], wn[l], wk[l],
+                                                        l == 3 ? RH_MLP_OUT : wn[l],
+                                                        l == 0 ? RH_MLP_IN : wk[l]);
+    }
+  }
+  const int B = n;
+  pack_inputs<<<blocks((int64_t)B * KIN, 256), 256, 0, st>>>(d_x, X0, B);
+  const __nv_bfloat16* in = X0;
+  for (int l = 0; l < 4; ++l) {
+    const int kin = wk[l], nout = wn[l];
+    const int tiles = ((B + 15) / 16) * ((nout + 7) / 8);
+    gemm_bf16<<<blocks((int64_t)tiles * 32, 128), 128, 0, st>>>(in, kin, 1, wbl[l], 1, kin, Z, nout,
+                                                                B, nout, kin, 0);
+    if (l < 3) {
+      bias_relu<<<blocks((int64_t)B * H, 256), 256, 0, st>>>(Z, bl[l], A, B, H);
+      in = A;
+    }
+  }
+  output_loss<<<blocks(B, 128), 128, 0, st>>>(Z, bl[3], nullptr, d_y, dz, dzb, nullptr, B);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    na_msg(err, err_len, "rh_mlp_forward_noalloc: launch failed: %s", cudaGetErrorString(e));
+    return RH_ERR_CUDA;
+  }
+  return RH_OK;
+}
