@@ -107,6 +107,9 @@ typedef struct {
                                  last lattice update for rh_get_state */
   int32_t window_steps;       /* steps per captured CUDA graph (0 = 100, one
                                  output period) */
+  int32_t cell_groups;        /* cells split into this many groups of about equal
+                                 CRU count that advance on concurrent streams
+                                 (0 = 4; capped at the number of cells) */
 } rh_run_opts;
 
 /* Full FP64 view of one cell's lattice state (caller-owned host arrays of

@@ -59,6 +59,7 @@ class RunOpts(C.Structure):
         ("stats_capacity", C.c_int32),
         ("keep_diagnostics", C.c_int32),
         ("window_steps", C.c_int32),
+        ("cell_groups", C.c_int32),
     ]
 
 

@@ -1,0 +1,460 @@
+// cellwarp.cuh — the whole-cell FP64 update (membrane_update and step_coef of
+// cellmodel.cuh) computed by one full warp.
+//
+// FP64 runs at a small fraction of the FP32 rate on this GPU, and a warp
+// instruction costs the FP64 pipe the same time whether one lane or 32 lanes
+// are active.  The serial versions evaluate some 55 exponentials, 60
+// divisions, three logarithms, two powers and three fmods one after the other
+// in one lane; here every group of mutually independent transcendentals and
+// divisions is evaluated in one SIMT call, one operand set per lane, through
+// a 32-slot shared-memory exchange.  Each operation keeps its operands and
+// its order, so the results are bit-identical to the serial versions (which
+// the CPU oracle restates); only the lane that computes each value changes.
+//
+// All 32 lanes of the calling warp must be active and call with identical
+// arguments; every lane returns the same results.
+#pragma once
+
+#include <math.h>
+
+#include "cellmodel.cuh"
+
+namespace rh {
+
+// Argument of one exponential of a per-lane table:
+//   u = {v, v - ek, XNAO}[src];  t = u + a;
+//   w = div ? t / d : t * c;  w = w * c2;  arg = sq ? (-w) * w : w
+// Each entry restates one exp() argument of membrane_update (the comment
+// gives the original form; (-x)/d equals x/(-d) and x - b equals x + (-b)
+// exactly in IEEE arithmetic, and x * 1 = x).
+struct ExpArg {
+  double a, c, d, c2;
+  int src, div, sq, pad;
+};
+
+enum { kSrcV = 0, kSrcVek = 1, kSrcNao = 2 };
+
+#define RH_MUL(c_, a_) {a_, c_, 1.0, 1.0, kSrcV, 0, 0, 0}
+#define RH_DIV(a_, d_) {a_, 1.0, d_, 1.0, kSrcV, 1, 0, 0}
+#define RH_NONE {0.0, 0.0, 1.0, 1.0, kSrcV, 0, 0, 0}
+
+// v < -40 mV (cuda_Cell_Detailed.cu:466-476 branch taken)
+__device__ const ExpArg kMemExpLow[32] = {
+    RH_MUL(-0.1, 47.13),                        // 0  am: -0.1*(v+47.13)
+    RH_DIV(0.0, -11.0),                         // 1  bm: -v/11
+    RH_DIV(80.0, -6.8),                         // 2  ah: (80+v)/(-6.8)
+    RH_MUL(0.079, 0.0),                         // 3  bh: 0.079*v
+    RH_MUL(0.35, 0.0),                          // 4  bh: 0.35*v
+    RH_MUL(0.2444, 0.0),                        // 5  aj: 0.2444*v
+    RH_MUL(-0.04391, 0.0),                      // 6  aj: -0.04391*v
+    RH_MUL(0.311, 79.23),                       // 7  aj: 0.311*(v+79.23)
+    RH_MUL(-0.01052, 0.0),                      // 8  bj: -0.01052*v
+    RH_MUL(-0.1378, 40.14),                     // 9  bj: -0.1378*(v+40.14)
+    RH_MUL(-0.123, 7.00),                       // 10 xkrv1: -0.123*(v+7)
+    RH_MUL(0.1450, 10.00),                      // 11 xkrv2: 0.145*(v+10)
+    RH_DIV(50.00, -7.50),                       // 12 xkrinf: -(v+50)/7.5
+    RH_DIV(33.00, 22.40),                       // 13 rg: (v+33)/22.4
+    RH_DIV(-1.500, -16.700),                    // 14 xs1ss: -(v-1.5)/16.7
+    RH_MUL(-0.1480, 30.0),                      // 15 tauxs: -0.148*(v+30)
+    RH_MUL(0.06870, 30.00),                     // 16 tauxs: 0.0687*(v+30)
+    {-59.215, 0.2385, 1.0, 1.0, kSrcVek, 0, 0, 0},   // 17 aki: 0.2385*(v-ek-59.215)
+    {5.476, 0.08032, 1.0, 1.0, kSrcVek, 0, 0, 0},    // 18 bki: 0.08032*(v-ek+5.476)
+    {-594.31, 0.061750, 1.0, 1.0, kSrcVek, 0, 0, 0}, // 19 bki: 0.06175*(v-ek-594.31)
+    {4.753, -0.5143, 1.0, 1.0, kSrcVek, 0, 0, 0},    // 20 bki: -0.5143*(v-ek+4.753)
+    RH_DIV(3.0, -15.00),                        // 21 rt1 = -(v+3)/15
+    RH_DIV(33.5, 10.00),                        // 22 rt2 = rt5 = (v+33.5)/10
+    RH_DIV(3.0, 15.00),                         // 23 -rt1
+    RH_DIV(60.00, 10.00),                       // 24 rt3 = (v+60)/10
+    {0.0, 1.0, 30.00, 1.0, kSrcV, 1, 1, 0},     // 25 rt4 = -(v/30)*(v/30)
+    {0.0, 1.0, 67.30, 1.0, kSrcNao, 1, 0, 0},   // 26 sigma: XNAO/67.3
+    {0.0, -0.1, 1.0, FRT, kSrcV, 0, 0, 0},      // 27 fnak: -0.1*v*FRT
+    RH_MUL(-FRT, 0.0),                          // 28 fnak: -v*FRT
+    RH_NONE, RH_NONE, RH_NONE};
+
+// v >= -40 mV: entries 2-4 are the other branch's, 5-9 unused
+__device__ const ExpArg kMemExpHigh[32] = {
+    RH_MUL(-0.1, 47.13),
+    RH_DIV(0.0, -11.0),
+    RH_DIV(10.66, -11.10),                      // 2  bh: (v+10.66)/(-11.1)
+    RH_MUL(-0.00000025350, 0.0),                // 3  bj: -2.535e-7*v
+    RH_MUL(-0.10, 32.00),                       // 4  bj: -0.1*(v+32)
+    RH_NONE, RH_NONE, RH_NONE, RH_NONE, RH_NONE,
+    RH_MUL(-0.123, 7.00),
+    RH_MUL(0.1450, 10.00),
+    RH_DIV(50.00, -7.50),
+    RH_DIV(33.00, 22.40),
+    RH_DIV(-1.500, -16.700),
+    RH_MUL(-0.1480, 30.0),
+    RH_MUL(0.06870, 30.00),
+    {-59.215, 0.2385, 1.0, 1.0, kSrcVek, 0, 0, 0},
+    {5.476, 0.08032, 1.0, 1.0, kSrcVek, 0, 0, 0},
+    {-594.31, 0.061750, 1.0, 1.0, kSrcVek, 0, 0, 0},
+    {4.753, -0.5143, 1.0, 1.0, kSrcVek, 0, 0, 0},
+    RH_DIV(3.0, -15.00),
+    RH_DIV(33.5, 10.00),
+    RH_DIV(3.0, 15.00),
+    RH_DIV(60.00, 10.00),
+    {0.0, 1.0, 30.00, 1.0, kSrcV, 1, 1, 0},
+    {0.0, 1.0, 67.30, 1.0, kSrcNao, 1, 0, 0},
+    {0.0, -0.1, 1.0, FRT, kSrcV, 0, 0, 0},
+    RH_MUL(-FRT, 0.0),
+    RH_NONE, RH_NONE, RH_NONE};
+
+#undef RH_MUL
+#undef RH_DIV
+#undef RH_NONE
+
+// 32-slot exchange of one warp: lane 0 deposits operands, every lane
+// evaluates its slot, every lane reads back any slot.
+struct WarpSlots {
+  double* n;  // [32] numerators / first operands
+  double* d;  // [32] denominators / second operands
+  double* r;  // [32] results
+  int lane;
+
+  // operands of slots 0..k-1 come from lane 0; the other slots get n = 0, d = 1
+  __device__ __forceinline__ void open(int k) {
+    __syncwarp();
+    if (lane >= k) {
+      n[lane] = 0.0;
+      d[lane] = 1.0;
+    }
+  }
+  __device__ __forceinline__ void put(int i, double a, double b) {
+    if (lane == 0) {
+      n[i] = a;
+      d[i] = b;
+    }
+  }
+  // every lane: its slot's quotient n/d, published in r
+  __device__ __forceinline__ void divide() {
+    __syncwarp();
+    const double q = n[lane] / d[lane];
+    r[lane] = q;
+    __syncwarp();
+  }
+  __device__ __forceinline__ double get(int i) const { return r[i]; }
+};
+
+// Membrane step (membrane_update, cellmodel.cuh) by one warp.  `s` is 160
+// doubles of shared memory owned by the warp.  The lattice sums come in as
+// tot (sum cs, sum xicat, sum xinaca over the cell's CRUs, :447-456); the
+// function also computes the three fmods of this step (stimulus phase and the
+// next lattice update's window flags) into fm[0..2].
+__device__ inline void membrane_update_warp(rh_membrane& m, double dt, double tperid,
+                                            double svikr, const double tot[3], int nin,
+                                            double* s, double fm[3]) {
+  const int lane = threadIdx.x & 31;
+  WarpSlots w{s, s + 32, s + 64, lane};
+  const double t = m.t, v = m.v;
+  const double xki = 140.0, xko = 5.40;  // :350-351
+  const double xnai = m.xnai;
+  const double prnak = 0.0183300;
+
+  // ---- round 0: reduction quotients, log and pow arguments ----
+  w.open(7);
+  w.put(0, XNAO, xnai);                                  // ena
+  w.put(1, xko, xki);                                    // ek
+  w.put(2, xko + prnak * XNAO, xki + prnak * xnai);      // eks
+  w.put(3, 12.00, xnai);                                 // INaK pow base
+  w.put(4, tot[0], (double)nin);                         // csubt (:447)
+  w.put(5, tot[1], CM);                                  // xicatto (:452)
+  w.put(6, tot[2], CM);                                  // xinacato (:456)
+  w.divide();
+  const double csubt = w.get(4);
+  m.csubt = csubt;
+  m.xicatto = w.get(5) * 0.0965 * VP * 2.0 * (ICAGAMMA + 1.);
+  m.xinacato = w.get(6) * 0.0965 * VS;
+  // logarithms (lanes 0-2)
+  const double lgv = log(w.r[lane]);
+  const double ena = (1.0 / FRT) * __shfl_sync(0xffffffffu, lgv, 0);
+  const double ek = (1.00 / FRT) * __shfl_sync(0xffffffffu, lgv, 1);
+  const double eks = (1.00 / FRT) * __shfl_sync(0xffffffffu, lgv, 2);
+  const double q12 = w.get(3);
+  // the IKs pow base needs csubt
+  w.open(1);
+  w.put(0, 0.28, csubt);
+  w.divide();
+  const double q28 = w.get(0);
+  // powers: lane 0 pow(0.28/csubt, 3), lane 1 pow(12/xnai, 1)
+  const double pw = pow(lane == 0 ? q28 : q12, lane == 0 ? 3.0 : 1.00);
+  const double pow_ks = __shfl_sync(0xffffffffu, pw, 0);
+  const double pow_nak = __shfl_sync(0xffffffffu, pw, 1);
+  // fmods: stimulus phase (:689) and the next update's window flags (:1244, :777)
+  {
+    const double tn = t + dt;
+    const double x = lane == 0 ? t + tperid - 100 : (lane == 1 ? tn - dt : tn + 0.0000001);
+    const double y = lane == 0 ? tperid : OUTT;
+    const double f = fmod(x, y);
+    fm[0] = __shfl_sync(0xffffffffu, f, 0);
+    fm[1] = __shfl_sync(0xffffffffu, f, 1);
+    fm[2] = __shfl_sync(0xffffffffu, f, 2);
+  }
+
+  // ---- round 1: the voltage exponentials, one per lane ----
+  double* const E = s + 96;  // E[i] = exp of table entry i
+  {
+    const ExpArg* tab = (v < -40.0) ? kMemExpLow : kMemExpHigh;
+    const ExpArg ea = tab[lane];
+    const double vek = v - ek;
+    const double u = ea.src == kSrcV ? v : (ea.src == kSrcVek ? vek : XNAO);
+    const double tt = u + ea.a;
+    const double q = tt / ea.d;
+    double z = ea.div ? q : tt * ea.c;
+    z = z * ea.c2;
+    const double arg = ea.sq ? (-z) * z : z;
+    const double ex = exp(arg);
+    __syncwarp();
+    E[lane] = ex;
+    __syncwarp();
+  }
+  const bool low = v < -40.0;
+
+  // ---- round 2: first-level divisions ----
+  const double bm = 0.08 * E[1];
+  double ah, bh, aj, bj, am;
+  w.open(20);
+  w.put(0, 0.32 * (v + 47.13), 1.0 - E[0]);                    // am
+  if (low) {
+    w.put(1, v + 37.78, 1.0 + E[7]);                           // aj factor
+    w.put(2, 0.1212 * E[8], 1.0 + E[9]);                       // bj
+  } else {
+    w.put(1, 1.00, 0.130 * (1.00 + E[2]));                     // bh
+    w.put(2, 0.3 * E[3], 1.0 + E[4]);                          // bj
+  }
+  w.put(3, 0.001380 * (v + 7.00), 1.0 - E[10]);                // xkrv1
+  w.put(4, 0.000610 * (v + 10.00), E[11] - 1.00);              // xkrv2
+  w.put(5, 1.00, 1.00 + E[12]);                                // xkrinf
+  w.put(6, 1.00, 1.00 + E[13]);                                // rg
+  w.put(7, 0.8, 1 + pow_ks);                                   // qks_inf term
+  w.put(8, 1.0, 1.0 + E[14]);                                  // xs1ss
+  w.put(9, 0.0000719 * (v + 30.00), 1.00 - E[15]);             // tauxs term 1
+  w.put(10, 0.0001310 * (v + 30.00), E[16] - 1.00);            // tauxs term 2
+  w.put(11, 1.02, 1.0 + E[17]);                                // aki
+  w.put(12, 0.49124 * E[18] + E[19], 1.0 + E[20]);             // bki
+  w.put(13, 1.00, 1.0 + E[21]);                                // xtos_inf
+  w.put(14, 1.00, 1.00 + E[22]);                               // ytos_inf = rs_inf
+  w.put(15, 9.00, 1.00 + E[23]);                               // txs
+  w.put(16, 3000.00, 1.0 + E[24]);                             // tys
+  w.put(17, 20.0, 1.0 + E[22]);                                // tyf
+  w.put(18, E[26] - 1.00, 7.00);                               // sigma
+  w.put(19, 1.0, 1.0 + pow_nak);                               // INaK factor
+  w.divide();
+  am = w.get(0);
+  if (low) {
+    ah = 0.135 * E[2];
+    bh = 3.56 * E[3] + 310000.0 * E[4];
+    aj = (-127140.0 * E[5] - 0.00003474 * E[6]) * w.get(1);
+    bj = w.get(2);
+  } else {
+    ah = 0.00;
+    bh = w.get(1);
+    aj = 0.00;
+    bj = w.get(2);
+  }
+  const double xkrv1 = w.get(3), xkrv2 = w.get(4), xkrinf = w.get(5), rg = w.get(6);
+  const double qks_inf = 0.2 * (1 + w.get(7));
+  const double xs1ss = w.get(8);
+  const double aki = w.get(11), bki = w.get(12);
+  const double xtos_inf = w.get(13), ytos_inf = w.get(14), rs_inf = w.get(14);
+  const double txs = w.get(15) + 0.50, tys = w.get(16) + 30.00;
+  const double txf = 3.50 * E[25] + 1.50, tyf = w.get(17) + 20.00;
+  const double sigma = w.get(18);
+  const double nak_f = w.get(19);
+  const double tauxs_sum = w.get(9) + w.get(10);
+
+  // ---- round 3: second-level divisions ----
+  const double tauqks = 1000.00;
+  w.open(11);
+  w.put(0, 1.00, ah + bh);                                     // tauh
+  w.put(1, 1.00, aj + bj);                                     // tauj
+  w.put(2, 1.00, am + bm);                                     // taum
+  w.put(3, ah, ah + bh);
+  w.put(4, aj, aj + bj);
+  w.put(5, am, am + bm);
+  w.put(6, 1.00, xkrv1 + xkrv2);                               // taukr
+  w.put(7, 1.00, tauxs_sum);                                   // tauxs
+  w.put(8, aki, aki + bki);                                    // xkin
+  w.put(9, 1.00, 1.0 + 0.1245 * E[27] + 0.0365 * sigma * E[28]);  // fnak
+  w.put(10, dt * (qks_inf - m.qks), tauqks);                   // qks increment
+  w.divide();
+  const double tauh = w.get(0), tauj = w.get(1), taum = w.get(2);
+  const double rh_ = w.get(3), rj_ = w.get(4), rm_ = w.get(5);
+  const double taukr = w.get(6);
+  const double tauxs = 0.95 * w.get(7);
+  const double xkin = w.get(8), fnak = w.get(9), dqks = w.get(10);
+
+  // ---- round 4: gate exponent arguments and INaK ----
+  w.open(10);
+  w.put(0, -dt, tauh);
+  w.put(1, -dt, tauj);
+  w.put(2, -dt, taum);
+  w.put(3, -dt, taukr);
+  w.put(4, -dt, tauxs);
+  w.put(5, -dt, txs);
+  w.put(6, -dt, tys);
+  w.put(7, -dt, txf);
+  w.put(8, -dt, tyf);
+  w.put(9, 1. * 1.5000 * fnak * nak_f * xko, xko + 1.50);      // xinak
+  w.divide();
+  const double xinak = w.get(9);
+  double* const G = s + 128;  // exp(-dt/tau) of the nine gates
+  {
+    const double ge = exp(lane < 9 ? w.r[lane] : 0.0);
+    G[lane] = ge;
+    __syncwarp();
+  }
+
+  // ---- serial remainder (identical in every lane) ----
+  const double gna = 15;
+  const double gnaleak = 0.3e-3 * 5;
+  const double xina = gna * m.xh * m.xj * m.xm * m.xm * m.xm * (v - ena) + gnaleak * (v - ena);
+  m.xh = rh_ - (rh_ - m.xh) * G[0];
+  m.xj = rj_ - (rj_ - m.xj) * G[1];
+  m.xm = rm_ - (rm_ - m.xm) * G[2];
+  const double gss = sqrt(xko / 5.40);
+  const double gkr = 0.0078360;
+  const double xikr = svikr * gkr * gss * m.xr * rg * (v - ek);
+  m.xr = xkrinf - (xkrinf - m.xr) * G[3];
+  const double gksx = 0.2000;
+  const double xiks = 1.0 * 1. * gksx * m.qks * m.xs1 * m.xs2 * (v - eks);
+  m.xs1 = xs1ss - (xs1ss - m.xs1) * G[4];
+  m.xs2 = xs1ss - (xs1ss - m.xs2) * G[4];
+  m.qks = m.qks + dqks;
+  const double gki = 0.600 * (sqrt(xko / 5.4));
+  const double xik1 = (1.0) * gki * xkin * (v - ek);
+  const double xitos = 1.0 * 0.040 * m.xtos * (m.ytos + 0.50 * rs_inf) * (v - ek);
+  m.xtos = xtos_inf - (xtos_inf - m.xtos) * G[5];
+  m.ytos = ytos_inf - (ytos_inf - m.ytos) * G[6];
+  const double xitof = 1.0 * 0.10 * m.xtof * m.ytof * (v - ek);
+  m.xtof = xtos_inf - (xtos_inf - m.xtof) * G[7];
+  m.ytof = ytos_inf - (ytos_inf - m.ytof) * G[8];
+  const double stim = (fm[0] < 1.0) ? 80.0 : 0.0;
+  const double wcainv = 1.0 / 50.0;
+  const double conv = 0.18 * 12500;
+  const double xrr = 1.0 * (1.0 / wcainv / conv) / 1000.0;
+  const double dnai = -xrr * (xina + 3.0 * xinak + 3.0 * m.xinacato);
+  m.xnai = xnai + dnai * dt;
+  const double dvh = -(xina + xik1 + 1 * xikr + 1 * xiks + xitos + 1 * xitof + 1. * m.xinacato +
+                       1 * m.xicatto + xinak) +
+                     stim;
+  m.v = v + dvh * dt;
+  m.out_ica += m.xicatto;
+  m.out_ncx += m.xinacato;
+  m.out_ina += xina;
+  m.xina = xina;
+  m.xiks = xiks;
+  m.xikr = xikr;
+  m.xik1 = xik1;
+  m.xinak = xinak;
+  m.xitos = xitos;
+  m.xitof = xitof;
+}
+
+// Coefficients of the next lattice update (step_coef, cellmodel.cuh) by one
+// warp; fm1, fm2 are fmod(t - dt, OUTT) and fmod(t + 1e-7, OUTT) for the
+// state's time t; `s` is 96 doubles of shared memory owned by the warp.
+// Returns whether the cell is inside its protocol.
+__device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
+                                      const CellConst& c, double dt, double fm1, double fm2,
+                                      double* s) {
+  const int lane = threadIdx.x & 31;
+  WarpSlots w{s, s + 32, s + 64, lane};
+  const double v = m.v, xnai = m.xnai, t = m.t;
+  double dv5 = 5, dvk = 8, fv5 = -22.8, fvk = 9.1;
+  k.alphac = 0.22;
+  k.betac = 4;
+  if (c.iso2) {
+    k.betac = 2;
+    dv5 = 0;
+    fv5 = -28;
+    fvk = 8.5;
+  }
+  // ---- round 1: quotients that do not need za ----
+  w.open(8);
+  w.put(0, v * FARAD, XRGAS);                  // za, first division
+  w.put(1, xnai, KMNAI);                       // r
+  w.put(2, 1.0, dt);                           // rdt
+  w.put(3, dt, 5.0);                           // dth
+  w.put(4, 0.95, dt);                          // rdt95
+  w.put(5, -(v - dv5), dvk);                   // dinf / taudin exponent
+  w.put(6, -(v - fv5), fvk);                   // finf exponent 1
+  w.put(7, (v - 60), 12.);                     // finf exponent 2
+  w.divide();
+  const double za1 = w.get(0), r = w.get(1);
+  k.rdt = w.get(2);
+  k.dth = w.get(3);
+  k.rdt95 = w.get(4);
+  const double x_d = w.get(5), x_f1 = w.get(6), x_f2 = w.get(7);
+  // ---- round 2: za, rdth95 ----
+  w.open(2);
+  w.put(0, za1, TEMPER);
+  w.put(1, 0.95, k.dth);
+  w.divide();
+  const double za = w.get(0);
+  k.rdth95 = w.get(1);
+  // ---- round 3: exponentials ----
+  const double tq = 0.0337 * (v + 10.5);
+  double X[7];
+  {
+    const double arg = lane == 0 ? x_d
+                     : lane == 1 ? x_f1
+                     : lane == 2 ? x_f2
+                     : lane == 3 ? -tq * tq
+                     : lane == 4 ? 2.0 * za
+                     : lane == 5 ? ETA * za
+                     : lane == 6 ? (ETA - 1.0) * za
+                                 : 0.0;
+    const double ex = exp(arg);
+#pragma unroll
+    for (int i = 0; i < 7; ++i) X[i] = __shfl_sync(0xffffffffu, ex, i);
+  }
+  const double e2z = X[4], e1 = X[5], e2 = X[6];
+  const bool za_small = fabs(za) < 0.001;
+  // ---- round 4 ----
+  w.open(5);
+  w.put(0, 1.0, 1.0 + X[0]);                                   // dinf
+  w.put(1, 1.0, 1.0 + X[1]);                                   // finf term
+  w.put(2, 1.0 - X[0], 0.035 * (v - dv5));                     // taudin inner
+  w.put(3, 4.0 * PCA * za * FARAD * GAMMAI, e2z - 1.0);        // lcc_k
+  w.put(4, e2z, 1000.0);                                       // lcc_e2z_k
+  w.divide();
+  const double dinf = w.get(0);
+  const double f_a = w.get(1), td_in = w.get(2);
+  k.lcc_k = za_small ? 2.0 * PCA * FARAD * GAMMAI : w.get(3);
+  k.lcc_e2z_k = w.get(4);
+  const bool v_tiny = (v < 0.0001) && (v > -0.0001);
+  // ---- round 5 ----
+  w.open(3);
+  w.put(0, f_a, 1. + X[2]);                                    // finf
+  w.put(1, 1.0, td_in * dinf);                                 // taudin
+  w.put(2, 0.035 * dvk, dinf);                                 // taudin near v = 0
+  w.divide();
+  const double finf = 1. - w.get(0);
+  const double taudin = v_tiny ? w.get(2) : w.get(1);
+  const double taufin = (0.02 - 0.007 * X[3]);
+  k.alphad = dinf * taudin;
+  k.betad = (1 - dinf) * taudin;
+  k.alphaf = finf * taufin;
+  k.betaf = (1 - finf) * taufin;
+  // NCX (subroutine_cuda.c:56-67)
+  const double xn3 = xnai * xnai * xnai;
+  k.ncx_num_a = e1 * xn3 * c.cao;
+  k.ncx_num_b = e2 * (XNAO * XNAO * XNAO);
+  k.ncx_t1 = KMCAI * (XNAO * XNAO * XNAO) * (1.0 + r * r * r);
+  k.ncx_t3a = (KMCAO + c.cao) * xn3;
+  k.ncx_den2 = 1.0 + KSAT * e2;
+  k.svica = c.svica;
+  k.svncx = c.svncx;
+  k.sviup = c.sviup_tot;
+  k.cao = c.cao;
+  k.ku = c.ku;
+  k.ku2 = c.ku2;
+  k.kb = c.kb;
+  k.dt = dt;
+  k.reset_window = fm1 < dt;
+  k.output_step = fm2 < dt;
+  return t < c.tend;
+}
+
+}  // namespace rh

@@ -120,8 +120,9 @@ struct StepArgs {
   Lattice<R> L;
   const CellConst* cells;
   CellDyn* dyn;
-  const int4* tiles;  // x: cell, y: first local CRU, z: CRUs in tile
-  double* partials;   // [tile][P_COUNT]
+  const int4* tiles;  // x: cell, y: first local CRU, z: CRUs in tile, w: arena index of that CRU
+  int tile_base;      // index of tiles[0] in the simulator's tile table (launches of one group)
+  double* partials;   // [tile][P_COUNT], by tile-table index
   double* out_wc;     // [cell][cap][45]
   double* out_ls;     // [ls_off + slot*lx + x][22]
   double* diag;       // optional

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -37,6 +38,14 @@ struct rh_sim {
     int4* d_tiles = nullptr;
   } sets[kNumTileSizes];
   int ts = 0;
+  // Cell groups: contiguous cell ranges of about equal CRU count, each with
+  // its own stream.  A window of steps runs as one graph with a branch per
+  // group, so one group's end-of-step tail (its last CTAs and the cell
+  // updates they run) overlaps the other groups' lattice work.
+  int ngroups = 1;
+  std::vector<int> group_cell;  // group g holds cells [group_cell[g], group_cell[g+1])
+  std::vector<cudaStream_t> gstreams;
+  std::vector<cudaEvent_t> gevents;  // [0] fork, [1..G] join
   int64_t stride = 0;
   int max_n = 0;
   int device = 0;
@@ -216,11 +225,48 @@ StepArgs<R> make_args(rh_sim* s, const Lattice<R>& L, bool lattice_only) {
   return a;
 }
 
-cudaError_t launch_one(rh_sim* s, bool out, bool lattice_only) {
+// One group's step: the tiles of cells [group_cell[g], group_cell[g+1]).
+cudaError_t launch_group(rh_sim* s, int g, bool out, bool lattice_only, cudaStream_t st) {
   const rh_sim::TileSet& t = s->sets[s->ts];
-  if (is_mixed(s))
-    return launch_step<float>(make_args(s, s->Lf, lattice_only), t.ntiles, out, t.tile, s->stream);
-  return launch_step<double>(make_args(s, s->Ld, lattice_only), t.ntiles, out, t.tile, s->stream);
+  const int tb = t.hcells[s->group_cell[g]].tile_begin;
+  const int te = s->group_cell[g + 1] < s->ncells ? t.hcells[s->group_cell[g + 1]].tile_begin
+                                                  : t.ntiles;
+  if (is_mixed(s)) {
+    StepArgs<float> a = make_args(s, s->Lf, lattice_only);
+    a.tiles += tb;
+    a.tile_base = tb;
+    return launch_step<float>(a, te - tb, out, t.tile, st);
+  }
+  StepArgs<double> a = make_args(s, s->Ld, lattice_only);
+  a.tiles += tb;
+  a.tile_base = tb;
+  return launch_step<double>(a, te - tb, out, t.tile, st);
+}
+
+// `n` steps of every group: group g's launches go to its own stream, forked
+// from and joined back to the simulator's stream (inside a capture this
+// makes one graph branch per group).
+cudaError_t launch_steps(rh_sim* s, int n, const bool* outs, bool lattice_only) {
+  if (s->ngroups == 1) {
+    for (int i = 0; i < n; ++i) {
+      cudaError_t e = launch_group(s, 0, outs[i], lattice_only, s->stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaEventRecord(s->gevents[0], s->stream);
+  for (int g = 0; g < s->ngroups && e == cudaSuccess; ++g) {
+    e = cudaStreamWaitEvent(s->gstreams[g], s->gevents[0], 0);
+    for (int i = 0; i < n && e == cudaSuccess; ++i)
+      e = launch_group(s, g, outs[i], lattice_only, s->gstreams[g]);
+    if (e == cudaSuccess) e = cudaEventRecord(s->gevents[1 + g], s->gstreams[g]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->gevents[1 + g], 0);
+  }
+  return e;
+}
+
+cudaError_t launch_one(rh_sim* s, bool out, bool lattice_only) {
+  return launch_steps(s, 1, &out, lattice_only);
 }
 
 bool out_step_host(double t, double dt) { return fmod(t + 0.0000001, OUTT) < dt; }
@@ -259,8 +305,9 @@ int run_window(rh_sim* s, int n, const std::vector<bool>& outs) {
   if (it == s->graphs.end()) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t le = cudaSuccess;
-    for (int i = 0; i < n && le == cudaSuccess; ++i) le = launch_one(s, outs[i], false);
+    std::unique_ptr<bool[]> o(new bool[n]);
+    for (int i = 0; i < n; ++i) o[i] = outs[i];
+    cudaError_t le = launch_steps(s, n, o.get(), false);
     cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
     if (le != cudaSuccess) return fail(s, RH_ERR_CUDA, "launch during capture: %s", cudaGetErrorString(le));
     if (ce != cudaSuccess) return fail(s, RH_ERR_CUDA, "capture: %s", cudaGetErrorString(ce));
@@ -363,7 +410,6 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   s->params.assign(cells, cells + ncells);
   // layout
   int64_t off = 0;
-  int tiles = 0;
   int64_t ls_off = 0;
   for (int c = 0; c < ncells; ++c) {
     const rh_cell_params& p = cells[c];
@@ -420,7 +466,8 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
       cc.tile_begin = nt;
       cc.tile_count = (cc.n + t.tile - 1) / t.tile;
       for (int q = 0; q < cc.tile_count; ++q)
-        t.htiles.push_back(make_int4(c, q * t.tile, std::min(t.tile, cc.n - q * t.tile), 0));
+        t.htiles.push_back(make_int4(c, q * t.tile, std::min(t.tile, cc.n - q * t.tile),
+                                     (int)(cc.off + (int64_t)q * t.tile)));
       nt += cc.tile_count;
     }
     t.ntiles = nt;
@@ -434,12 +481,35 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     if (s->ts < 0) return fail(s, RH_ERR_ARG, "block_size %d is not a compiled tile length", want);
   }
   s->hcells = s->sets[s->ts].hcells;
-  (void)tiles;
+  if (off > INT32_MAX - 256) return fail(s, RH_ERR_ARG, "ensemble too large (%lld CRUs)", (long long)off);
   s->stride = off;
   s->ls_rows_total = ls_off;
   s->device = s->opts.device;
   CK(cudaSetDevice(s->device));
+  CK(prepare_step_kernels());
   CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  {
+    // cell groups of about equal CRU count (never more groups than cells)
+    int want = s->opts.cell_groups > 0 ? s->opts.cell_groups : kDefaultGroups;
+    want = std::max(1, std::min(want, ncells));
+    int64_t total = 0;
+    for (const CellConst& c : s->hcells) total += c.n;
+    s->group_cell.assign(1, 0);
+    int64_t acc = 0;
+    for (int c = 0; c < ncells; ++c) {
+      acc += s->hcells[c].n;
+      const int g = (int)s->group_cell.size();  // next boundary index
+      if (g < want && c + 1 < ncells && acc * want >= total * g) s->group_cell.push_back(c + 1);
+    }
+    s->ngroups = (int)s->group_cell.size();
+    s->group_cell.push_back(ncells);
+    if (s->ngroups > 1) {
+      s->gstreams.resize(s->ngroups);
+      s->gevents.resize(s->ngroups + 1);
+      for (auto& st : s->gstreams) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+      for (auto& ev : s->gevents) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+  }
   CK(cudaEventCreate(&s->ev0));
   CK(cudaEventCreate(&s->ev1));
   s->arena_bytes = lattice_bytes(real_size(s), s->stride);
@@ -521,6 +591,10 @@ int rh_destroy(rh_sim* s) {
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
+  for (cudaStream_t st : s->gstreams)
+    if (st) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : s->gevents)
+    if (ev) cudaEventDestroy(ev);
   delete s;
   return RH_OK;
 }
@@ -565,10 +639,10 @@ int rh_run_steps(rh_sim* s, int64_t nsteps) {
       r = run_window(s, k, outs);
     } else {
       r = RH_OK;
-      for (int i = 0; i < k; ++i) {
-        cudaError_t e = launch_one(s, outs[i], false);
-        if (e != cudaSuccess) return fail(s, RH_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
-      }
+      std::unique_ptr<bool[]> o(new bool[k]);
+      for (int i = 0; i < k; ++i) o[i] = outs[i];
+      cudaError_t e = launch_steps(s, k, o.get(), false);
+      if (e != cudaSuccess) return fail(s, RH_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
     }
     if (r) return r;
     nlaunch += k;

@@ -20,9 +20,11 @@
 #include <stdint.h>
 
 #include "cellmodel.cuh"
+#include "cellwarp.cuh"
 #include "lattice.cuh"
 #include "model.cuh"
 #include "step.cuh"
+#include "tma.cuh"
 
 namespace rh {
 
@@ -82,9 +84,11 @@ __device__ __forceinline__ R clamp0(R x) {
 
 // ------------------------------------------------------------ cell update
 
-// Whole-cell part of the step, run by warp 0 of the last CTA of the cell.
+// Whole-cell part of the step, run by warp 0 (all 32 lanes) of the last CTA
+// of the cell.  `scratch` is 160 doubles of shared memory no longer used by
+// the tile.
 template <class R>
-__device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step) {
+__device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step, double* scratch) {
   const int lane = threadIdx.x & 31;
   CellDyn* dyn = a.dyn + cell;
   const CellConst& cc = a.cells[cell];
@@ -104,7 +108,7 @@ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step) {
     double ws, wc;
     warp_sum_comp(s, ws, wc);
     double wc2 = warp_sum(c);
-    tot[q] = ws + (wc + wc2);
+    tot[q] = __shfl_sync(0xffffffffu, ws + (wc + wc2), 0);
   }
   double osum[NOUT];
   if (out_step) {
@@ -122,55 +126,78 @@ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step) {
     for (int off = 16; off > 0; off >>= 1) f = fmax(f, __shfl_down_sync(0xffffffffu, f, off));
     osum[O_CIHIGH - P_STEP_END] = f;
   }
-  if (lane != 0) return;
   rh_membrane m = dyn->m;
   const double dt = a.dt;
-  // reduction (:447-456)
-  m.csubt = tot[0] / cc.n;
-  m.xicatto = tot[1] / CM * 0.0965 * VP * 2.0 * (ICAGAMMA + 1.);
-  m.xinacato = tot[2] / CM * 0.0965 * VS;
-  membrane_update(m, dt, cc.pcl, cc.svikr);
+  // reduction (:447-456) and membrane model (:458-739), warp-parallel
+  double fm[3];
+  membrane_update_warp(m, dt, cc.pcl, cc.svikr, tot, cc.n, scratch, fm);
   uint32_t status = dyn->status;
   if (!isfinite(m.v) || !isfinite(m.xnai) || !isfinite(m.csubt) || !isfinite(m.xicatto) ||
       !isfinite(m.xinacato))
     status |= RH_STATUS_NAN;
-  if (a.stats) {  // per-beat detectors on the (t, V) sample of this step
-    rh_beat_stats rec;
-    if (beat_on_step(dyn->bt, m.t, m.v, cc.pcl, &rec)) {
-      a.stats[(size_t)cell * a.stats_cap + dyn->stats_count % a.stats_cap] = rec;
-      dyn->stats_count += 1;
+  if (lane == 0) {
+    if (a.stats) {  // per-beat detectors on the (t, V) sample of this step
+      rh_beat_stats rec;
+      if (beat_on_step(dyn->bt, m.t, m.v, cc.pcl, &rec)) {
+        a.stats[(size_t)cell * a.stats_cap + dyn->stats_count % a.stats_cap] = rec;
+        dyn->stats_count += 1;
+      }
     }
-  }
-  if (out_step) {
-    m.sparksum += (long long)osum[O_SPARK - P_STEP_END];
-    if (osum[O_CIHIGH - P_STEP_END] > 0) status |= RH_STATUS_CI_HIGH;
-    long long slot = dyn->out_count % a.out_cap;
-    double* w = a.out_wc + ((size_t)cell * a.out_cap + slot) * RH_WHOLECELL_COLS;
-    wholecell_columns(w, osum, m, cc.n, dt);
-    if (a.stats) beat_on_output(dyn->bt, w);
-    dyn->out_count += 1;
-    m.sparksum = 0;  // :1074-1077
-    m.out_ica = 0;
-    m.out_ncx = 0;
-    m.out_ina = 0;
+    if (out_step) {
+      m.sparksum += (long long)osum[O_SPARK - P_STEP_END];
+      if (osum[O_CIHIGH - P_STEP_END] > 0) status |= RH_STATUS_CI_HIGH;
+      long long slot = dyn->out_count % a.out_cap;
+      double* w = a.out_wc + ((size_t)cell * a.out_cap + slot) * RH_WHOLECELL_COLS;
+      wholecell_columns(w, osum, m, cc.n, dt);
+      if (a.stats) beat_on_output(dyn->bt, w);
+      dyn->out_count += 1;
+      m.sparksum = 0;  // :1074-1077
+      m.out_ica = 0;
+      m.out_ncx = 0;
+      m.out_ina = 0;
+    }
   }
   m.t = m.t + dt;  // :1083
   m.step += 1;
   StepCoef<double> kd;
-  bool active = step_coef(kd, m, cc, dt);
-  StepCoef<float> kf;
-  convert_coef(kf, kd);
-  if (!active) {
-    dyn->done = 1;
-    status |= RH_STATUS_DONE;
+  const bool active = step_coef_warp(kd, m, cc, dt, fm[1], fm[2], scratch);
+  if (lane == 0) {
+    StepCoef<float> kf;
+    convert_coef(kf, kd);
+    if (!active) {
+      dyn->done = 1;
+      status |= RH_STATUS_DONE;
+    }
+    dyn->m = m;
+    dyn->cd = kd;
+    dyn->cf = kf;
+    dyn->status = status;
   }
-  dyn->m = m;
-  dyn->cd = kd;
-  dyn->cf = kf;
-  dyn->status = status;
 }
 
 // ------------------------------------------------------------- step kernel
+
+// Dynamic shared memory of one CTA (tile of B CRUs).  Always the z-pair
+// planes of ci and cnsr, which the stencil reads from neighbouring threads.
+// FP32 kernels also stage every other field of the tile's CRUs with
+// asynchronous copies issued at the top of the kernel, so a thread's whole
+// state arrives in one batch (the copies of the fields updated in place
+// overlap the cell-header load); the FP64 kernels are bound by the FP64
+// pipe, not by memory latency, and read those fields directly.
+template <class R, int B>
+struct TileSmem {
+  using V = typename Vec2<R>::T;
+  static constexpr bool kStage = sizeof(R) == 4;
+  static constexpr size_t kPlane = sizeof(V) * B;     // one pair plane
+  static constexpr size_t kCi = 0;                     // V[4][B]
+  static constexpr size_t kCn = 4 * kPlane;            // V[4][B]
+  static constexpr size_t kBuf = 8 * kPlane;           // V[6][4][B]: catf cats cacal casr camyo mgmyo
+  static constexpr size_t kSc = kBuf + 24 * kPlane;    // R[9][B]: cp cjsr cjsrb ancx casar casarh casarj casarhj cs
+  static constexpr size_t kLcc = kSc + 9 * sizeof(R) * B;  // uint2[B]
+  static constexpr size_t kRyr = kLcc + 8 * B;             // u32[B]
+  static constexpr size_t kWin = kRyr + 4 * B;             // u32[B]
+  static constexpr size_t kBytes = kStage ? kWin + 4 * B : kBuf;
+};
 
 struct TileHeader {
   int lx, ly, lz, nxf, nyf, tile_count, line_y, line_z;
@@ -183,11 +210,19 @@ struct TileHeader {
 template <class R, bool OUT, int B>
 __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArgs<R> a) {
   constexpr int kBlock = B;
+  using TS = TileSmem<R, B>;
+  constexpr bool kStage = TS::kStage;
   __shared__ TileHeader sh;
   __shared__ StepCoef<R> sk;
   using V = typename Vec2<R>::T;
-  __shared__ V s_ci2[4][kBlock];
-  __shared__ V s_cn2[4][kBlock];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  V(*s_ci2)[kBlock] = reinterpret_cast<V(*)[kBlock]>(dsm + TS::kCi);
+  V(*s_cn2)[kBlock] = reinterpret_cast<V(*)[kBlock]>(dsm + TS::kCn);
+  V(*s_buf)[4][kBlock] = reinterpret_cast<V(*)[4][kBlock]>(dsm + TS::kBuf);
+  R(*s_sc)[kBlock] = reinterpret_cast<R(*)[kBlock]>(dsm + TS::kSc);
+  uint2* s_lcc = reinterpret_cast<uint2*>(dsm + TS::kLcc);
+  uint32_t* s_ryr = reinterpret_cast<uint32_t*>(dsm + TS::kRyr);
+  uint32_t* s_win = reinterpret_cast<uint32_t*>(dsm + TS::kWin);
   __shared__ double s_red[kBlock / 32][P_COUNT];
   __shared__ uint32_t s_status;
   __shared__ int s_last;
@@ -195,6 +230,43 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   const int4 tile = a.tiles[blockIdx.x];
   const int cell = tile.x;
   const int tid = threadIdx.x;
+  const int cpad = (tile.z + 31) & ~31;  // cells are padded to 32 CRUs
+  const int64_t gt0 = (int64_t)(uint32_t)tile.w;  // arena index of the tile's first CRU
+  if (kStage) {
+    // Fields updated in place do not depend on the ping-pong parity, so
+    // their copies start before the cell header arrives.  16-byte chunks:
+    // a pair plane holds 2 CRUs per chunk, a 4-byte plane 4.
+    const Lattice<R>& L = a.L;
+    const int64_t S = L.stride;
+    constexpr int kTpp = kBlock / 2;  // threads per pair plane
+    const int c2 = tid % kTpp, h2 = tid / kTpp;
+    if (2 * c2 < cpad) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {  // 6 buffers x 4 pair planes, two planes per round
+        const int f = k >> 1, pl = 2 * (k & 1) + h2;
+        const R* base = f == 0 ? L.catf : f == 1 ? L.cats : f == 2 ? L.cacal
+                      : f == 3 ? L.casr : f == 4 ? L.camyo : L.mgmyo;
+        cp_async16(&s_buf[f][pl][2 * c2],
+                   reinterpret_cast<const V*>(base) + pl * S + gt0 + 2 * c2);
+      }
+      if (h2 == 0) cp_async16(&s_lcc[2 * c2], L.lcc + gt0 + 2 * c2);
+    }
+    constexpr int kTpq = kBlock / 4;  // threads per 4-byte plane
+    const int c4 = tid % kTpq, h4 = tid / kTpq;
+    if (4 * c4 < cpad) {
+#pragma unroll
+      for (int f = 0; f < 10; ++f) {  // cp cjsr cjsrb ancx casar casarh casarj casarhj ryr win
+        if ((f & 3) != h4) continue;
+        const void* src = f == 0 ? (const void*)(L.cp + gt0) : f == 1 ? (const void*)(L.cjsr + gt0)
+                        : f == 2 ? (const void*)(L.cjsrb + gt0) : f == 3 ? (const void*)(L.ancx + gt0)
+                        : f == 4 ? (const void*)(L.casar + gt0) : f == 5 ? (const void*)(L.casarh + gt0)
+                        : f == 6 ? (const void*)(L.casarj + gt0) : f == 7 ? (const void*)(L.casarhj + gt0)
+                        : f == 8 ? (const void*)(L.ryr + gt0) : (const void*)(L.win + gt0);
+        void* dst = f < 8 ? (void*)&s_sc[f][4 * c4] : f == 8 ? (void*)&s_ryr[4 * c4] : (void*)&s_win[4 * c4];
+        cp_async16(dst, static_cast<const char*>(src) + 16 * c4);
+      }
+    }
+  }
   {
     const CellDyn* d = a.dyn + cell;
     const int* src = reinterpret_cast<const int*>(coef_ptr<R>(d));
@@ -223,7 +295,10 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     }
   }
   __syncthreads();
-  if (sh.done) return;
+  if (sh.done) {
+    if (kStage) cp_async_wait_all();  // no copy may still target this CTA's shared memory
+    return;
+  }
 
   const bool out_step = OUT && sk.output_step && !a.lattice_only;
   const Lattice<R>& L = a.L;
@@ -239,10 +314,26 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   const V* cn2 = reinterpret_cast<const V*>(L.cnsr[par]);
 
   // ---- stage the tile's own sub-voxels (z-pairs) ----
+  if (kStage) {
+    constexpr int kTpp = kBlock / 2;
+    const int c2 = tid % kTpp, h2 = tid / kTpp;
+    if (2 * c2 < cpad) {
 #pragma unroll
-  for (int p = 0; p < 4; ++p) {
-    s_ci2[p][tid] = valid ? ci2[p * S + g] : splat2(R(0));
-    s_cn2[p][tid] = valid ? cn2[p * S + g] : splat2(R(0));
+      for (int k = 0; k < 4; ++k) {  // ci and cnsr, 4 pair planes each
+        const int pl = 2 * (k & 1) + h2;
+        const V* src = (k >> 1) ? cn2 : ci2;
+        V(*dst)[kBlock] = (k >> 1) ? s_cn2 : s_ci2;
+        cp_async16(&dst[pl][2 * c2], src + pl * S + gt0 + 2 * c2);
+      }
+    }
+    if (4 * tid < cpad) cp_async16(&s_sc[8][4 * tid], L.cs[par] + gt0 + 4 * tid);
+    cp_async_wait_all();
+  } else {
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      s_ci2[p][tid] = valid ? ci2[p * S + g] : splat2(R(0));
+      s_cn2[p][tid] = valid ? cn2[p * S + g] : splat2(R(0));
+    }
   }
   __syncthreads();
 
@@ -262,8 +353,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     V* cnnext2 = reinterpret_cast<V*>(L.cnsr[par ^ 1]);
     R* csnext = L.cs[par ^ 1];
 
-    R cp = L.cp[g], cjsr = L.cjsr[g];
-    const R cs0 = cs[g];
+    R cp = kStage ? s_sc[0][tid] : L.cp[g], cjsr = kStage ? s_sc[1][tid] : L.cjsr[g];
+    const R cs0 = kStage ? s_sc[8][tid] : cs[g];
     // ---- dyad/submembrane/JSR coupling terms from the old state (:1309-1314) ----
     const R ci0 = s_ci2[0][tid].x, ci1 = s_ci2[0][tid].y;
     const R cn0 = s_cn2[0][tid].x, cn1 = s_cn2[0][tid].y;
@@ -394,8 +485,9 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       }
       // cytosolic buffers (buffers.c:55-115): on*(B-b) - koff*b, with the
       // saturation guard kon*c*dt > 1 taken on the rare slow path
-      V catf = catf2[gp], cats = cats2[gp], cacal = cacal2[gp], casr = casr2[gp];
-      V camyo = camyo2[gp], mgmyo = mgmyo2[gp];
+      V catf = kStage ? s_buf[0][p][tid] : catf2[gp], cats = kStage ? s_buf[1][p][tid] : cats2[gp];
+      V cacal = kStage ? s_buf[2][p][tid] : cacal2[gp], casr = kStage ? s_buf[3][p][tid] : casr2[gp];
+      V camyo = kStage ? s_buf[4][p][tid] : camyo2[gp], mgmyo = kStage ? s_buf[5][p][tid] : mgmyo2[gp];
       const V freemyo = vsub(vsub(splat2(R(BMYO)), camyo), mgmyo);
       V r_tf = vfma(vmul(splat2(R(KTFON)), c), vsub(splat2(R(BTF)), catf), vmul(splat2(R(-KTFOFF)), catf));
       V r_ts = vfma(vmul(splat2(R(KTSON)), c), vsub(splat2(R(BTS)), cats), vmul(splat2(R(-KTSOFF)), cats));
@@ -474,10 +566,10 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     }
 
     // ---- CRU state of the stochastic part ----
-    R cjsrb = L.cjsrb[g], ancx = L.ancx[g];
-    const uint32_t ryr = L.ryr[g];
-    uint2 lccw = L.lcc[g];
-    const uint32_t win = L.win[g];
+    R cjsrb = kStage ? s_sc[2][tid] : L.cjsrb[g], ancx = kStage ? s_sc[3][tid] : L.ancx[g];
+    const uint32_t ryr = kStage ? s_ryr[tid] : L.ryr[g];
+    uint2 lccw = kStage ? s_lcc[tid] : L.lcc[g];
+    const uint32_t win = kStage ? s_win[tid] : L.win[g];
     int nou = ryr & 0xff, ncu = (ryr >> 8) & 0xff, nob = (ryr >> 16) & 0xff, ncb = ryr >> 24;
     int nl = win & 0xffff, nspark = win >> 16;
     if (k.reset_window) {  // :1244-1247
@@ -553,12 +645,14 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     cjsrb += (R(1) - beta) * jterm * dt;
 
     // ---- five sub-steps of cs, cp and the sarcolemmal buffers (:1396-1473) ----
-    R casar = L.casar[g], casarh = L.casarh[g], casarj = L.casarj[g], casarhj = L.casarhj[g];
+    R casar = kStage ? s_sc[4][tid] : L.casar[g], casarh = kStage ? s_sc[5][tid] : L.casarh[g];
+    R casarj = kStage ? s_sc[6][tid] : L.casarj[g], casarhj = kStage ? s_sc[7][tid] : L.casarhj[g];
     R csn = cs0;
     {
       const R dth = k.dth, rdth95 = k.rdth95;
-      const R csN = has_zp ? __ldg(cs + g + lxly) : cs0;
-      const R csS = has_zm ? __ldg(cs + g - lxly) : cs0;
+      R csN = cs0, csS = cs0;
+      if (has_zp) csN = (kStage && tid + lxly < count) ? s_sc[8][tid + lxly] : __ldg(cs + g + lxly);
+      if (has_zm) csS = (kStage && tid - lxly >= 0) ? s_sc[8][tid - lxly] : __ldg(cs + g - lxly);
       const R csdiff = (csN + csS - R(2) * cs0) * R(1.0 / TAUST);
       const R cs_const = -R(ICAGAMMA * VP / VS) * icat1 + xinaca -
                          (cs0 - ci0) * R(1.0 / TAUSI / 2.) - (cs0 - ci1) * R(1.0 / TAUSI / 2.) +
@@ -722,7 +816,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   __syncthreads();
   if (tid < 32) {
     constexpr int NW = kBlock / 32;
-    double* dst = a.partials + (size_t)blockIdx.x * P_COUNT;
+    double* dst = a.partials + (size_t)(a.tile_base + blockIdx.x) * P_COUNT;
     if (lane < 3) {
       // compensated sum over warps in fixed order
       double s = 0.0, c = 0.0;
@@ -760,7 +854,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   // ---- last CTA of the cell: whole-cell update ----
   if (tid < 32) {
     __threadfence();
-    if (!a.lattice_only) cell_update<R>(a, cell, out_step);
+    if (!a.lattice_only) cell_update<R>(a, cell, out_step, reinterpret_cast<double*>(dsm));
     if (tid == 0) {
       a.dyn[cell].parity = par ^ 1;
       a.dyn[cell].arrive = 0;
@@ -832,12 +926,36 @@ __global__ void coef_prep_kernel(const CellConst* cells, CellDyn* dyn, int ncell
 
 // ------------------------------------------------------------- launchers
 
+// Instantiations whose tile needs more than the default 48 KB of dynamic
+// shared memory opt in once per device (before any launch or capture).
+template <class R, int B>
+cudaError_t opt_in_smem() {
+  constexpr size_t smem = TileSmem<R, B>::kBytes;
+  if (smem <= 48 * 1024) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(step_kernel<R, true, B>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(step_kernel<R, false, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem);
+}
+
+cudaError_t prepare_step_kernels() {
+  cudaError_t e;
+  if ((e = opt_in_smem<float, 64>()) != cudaSuccess) return e;
+  if ((e = opt_in_smem<float, 128>()) != cudaSuccess) return e;
+  if ((e = opt_in_smem<float, 256>()) != cudaSuccess) return e;
+  if ((e = opt_in_smem<double, 64>()) != cudaSuccess) return e;
+  if ((e = opt_in_smem<double, 128>()) != cudaSuccess) return e;
+  return opt_in_smem<double, 256>();
+}
+
 template <class R, int B>
 void launch_b(const StepArgs<R>& a, int ntiles, bool out, cudaStream_t st) {
+  constexpr size_t smem = TileSmem<R, B>::kBytes;
   if (out)
-    step_kernel<R, true, B><<<ntiles, B, 0, st>>>(a);
+    step_kernel<R, true, B><<<ntiles, B, smem, st>>>(a);
   else
-    step_kernel<R, false, B><<<ntiles, B, 0, st>>>(a);
+    step_kernel<R, false, B><<<ntiles, B, smem, st>>>(a);
 }
 
 template <class R>

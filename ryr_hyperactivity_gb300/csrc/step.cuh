@@ -13,6 +13,10 @@ constexpr int kNumTileSizes = 3;
 constexpr int kTileSizes[kNumTileSizes] = {64, 128, 256};
 constexpr int kDefaultTile = 128;
 
+// Cell groups advanced on concurrent streams when the run options leave the
+// choice to the library.
+constexpr int kDefaultGroups = 4;
+
 // Resident CTAs per SM each instantiation's register allocation is bounded
 // for.  FP32: about 640 threads per SM at <= ~100 registers (measured best:
 // the kernel is latency-bound and wants warps).  FP64: bound by the FP64 pipe,
@@ -39,6 +43,10 @@ cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, int tile, cu
 template <class R>
 cudaError_t launch_init(const Lattice<R>& L, const CellConst* cells, const InitValues* iv,
                         int ncells, int max_n, cudaStream_t st);
+
+// Per-device set-up of the step kernels (shared-memory opt-in); call with
+// the device current before the first launch.
+cudaError_t prepare_step_kernels();
 
 cudaError_t launch_volt_prep(const CellConst* cells, CellDyn* dyn, int ncells, double dt,
                              cudaStream_t st);

@@ -1,5 +1,6 @@
-// tma.cuh — bulk asynchronous copies (the TMA unit's 1-D cp.async.bulk) from
-// global to shared memory, completed on an mbarrier, with bounded waits.
+// tma.cuh — asynchronous copies from global to shared memory: per-thread
+// 16-byte cp.async (completed with cp.async.wait_all) and the TMA unit's 1-D
+// cp.async.bulk (completed on an mbarrier, with bounded waits).
 //
 // Rules kept here: both addresses 16-byte aligned, sizes multiples of 16
 // bytes, the mbarrier initialised and fenced before any copy names it, and
@@ -36,6 +37,28 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
           "r"(smem_addr(dst)),
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
+}
+
+// One thread's 16-byte global -> shared copy (both addresses 16-byte
+// aligned); L1 is bypassed (.cg), the data goes straight to shared memory.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src)
+               : "memory");
+}
+
+// Waits until every cp.async this thread issued has landed in shared memory
+// (other threads' copies need a barrier after their own wait).
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// Copies `bytes` (a multiple of 16) from src to dst with the CTA's NT
+// threads, 16 bytes per thread and round.
+template <int NT>
+__device__ __forceinline__ void cp_async_region(void* dst, const void* src, int bytes, int tid) {
+  char* d = static_cast<char*>(dst);
+  const char* s = static_cast<const char*>(src);
+  for (int i = tid * 16; i < bytes; i += NT * 16) cp_async16(d + i, s + i);
 }
 
 // Polls the barrier's phase `parity` at most `max_polls` times; returns 1 when

@@ -20,7 +20,10 @@ def run_opts(precision: str = "fp64", **kw) -> RunOpts:
     o = RunOpts()
     L.rh_default_run_opts(C.byref(o))
     o.precision = PRECISIONS[precision]
+    names = {f[0] for f in RunOpts._fields_}
     for k, v in kw.items():
+        if k not in names:
+            raise TypeError(f"unknown run option {k!r}")
         setattr(o, k, v)
     return o
 
