@@ -236,9 +236,15 @@ int rh_tile_size(const rh_sim* sim, int32_t* tile_crus);
  * simulator's precision (each persistent field read once, written once). */
 int rh_bytes_per_cru_step(const rh_sim* sim, double* bytes);
 
-/* Device time of the lattice-update kernels, accumulated since the last call
- * (CUDA events on the simulator's stream); returns launches and milliseconds. */
+/* Device time of the lattice updates, accumulated since the last call (CUDA
+ * events on the simulator's stream around the work it enqueued); returns the
+ * number of lattice updates (time steps) and milliseconds.  Each update is
+ * one step-kernel launch per cell group (rh_num_groups). */
 int rh_kernel_timing(rh_sim* sim, int64_t* launches, double* ms);
+
+/* Number of cell groups advanced on concurrent streams (run option
+ * cell_groups, capped at the number of cells). */
+int rh_num_groups(const rh_sim* sim, int32_t* groups);
 
 /* Copies the text of the last error into buf (always NUL-terminated). */
 int rh_last_error(const rh_sim* sim, char* buf, size_t n);

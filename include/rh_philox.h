@@ -45,15 +45,11 @@ typedef struct {
   uint32_t w[4];
 } rh_u32x4;
 
+/* One 32x32 -> 64-bit product (a single wide multiply on the GPU). */
 RH_HD void rh_mulhilo32(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo) {
-#if defined(__CUDA_ARCH__)
-  *hi = __umulhi(a, b);
-  *lo = a * b;
-#else
   uint64_t p = (uint64_t)a * (uint64_t)b;
   *hi = (uint32_t)(p >> 32);
   *lo = (uint32_t)p;
-#endif
 }
 
 /* Philox4x32 with 10 rounds: counter (c0..c3), key (k0, k1). */

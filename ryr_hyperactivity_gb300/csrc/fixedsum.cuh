@@ -1,0 +1,104 @@
+// fixedsum.cuh — exact whole-cell sums in 128-bit fixed point.
+//
+// The three sums every time step needs (cs, xicat, xinaca over the cell's
+// CRUs, cuda_Cell_Detailed.cu:435-456) are accumulated as value * 2^64 in
+// two's-complement 128-bit integers.  FP32 values in the model's range
+// (|v| < 2^40, magnitudes down to 2^-64) convert exactly, FP64 values are
+// truncated below 2^-64; integer addition is exact and associative, so every
+// CTA adds its tile's sum to the cell's accumulator with integer atomics in
+// any order and the result is the same bits every run.  The cell update
+// converts the total to FP64 with one rounding.  No FP64 arithmetic runs in
+// the lattice CTAs, where it would cost the slow FP64 pipe.
+#pragma once
+
+#include <stdint.h>
+
+namespace rh {
+
+// Magnitudes at or above 2^kFxMaxExp are reported as invalid (the model's
+// concentrations and currents are many orders below it).
+constexpr int kFxMaxExp = 40;
+
+__device__ __forceinline__ void fx_neg(uint64_t& lo, uint64_t& hi) {
+  lo = ~lo + 1ull;
+  hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+}
+
+// v * 2^64 as (lo, hi), truncated toward zero; `bad` is set for non-finite
+// values and |v| >= 2^kFxMaxExp (the result is then 0).
+__device__ __forceinline__ void fx_from(float v, uint64_t& lo, uint64_t& hi, uint32_t& bad) {
+  const uint32_t b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xffu);
+  const uint64_t m = (uint64_t)((b & 0x7fffffu) | 0x800000u);  // 24 bits
+  lo = 0ull;
+  hi = 0ull;
+  if (e >= 127 + kFxMaxExp) {  // also Inf and NaN (e = 255)
+    bad = 1u;
+    return;
+  }
+  if (e == 0) return;  // zero or subnormal: below 2^-126, under the resolution
+  const int s = e - 86;  // v * 2^64 = m * 2^s, s < 81
+  if (s >= 64) {
+    hi = m << (s - 64);
+  } else if (s >= 0) {
+    lo = m << s;
+    hi = s > 40 ? (m >> (64 - s)) : 0ull;
+  } else if (s > -24) {
+    lo = m >> (-s);
+  }
+  if (b >> 31) fx_neg(lo, hi);
+}
+
+__device__ __forceinline__ void fx_from(double v, uint64_t& lo, uint64_t& hi, uint32_t& bad) {
+  const uint64_t b = (uint64_t)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ffull);
+  const uint64_t m = (b & 0xfffffffffffffull) | 0x10000000000000ull;  // 53 bits
+  lo = 0ull;
+  hi = 0ull;
+  if (e >= 1023 + kFxMaxExp) {
+    bad = 1u;
+    return;
+  }
+  if (e == 0) return;
+  const int s = e - 1011;  // v * 2^64 = m * 2^s, s < 52
+  if (s >= 0) {
+    lo = m << s;
+    hi = s > 11 ? (m >> (64 - s)) : 0ull;
+  } else if (s > -53) {
+    lo = m >> (-s);
+  }
+  if (b >> 63) fx_neg(lo, hi);
+}
+
+__device__ __forceinline__ void fx_add(uint64_t& lo, uint64_t& hi, uint64_t lo2, uint64_t hi2) {
+  const uint64_t l = lo + lo2;
+  hi = hi + hi2 + (l < lo ? 1ull : 0ull);
+  lo = l;
+}
+
+// Warp sum; the total is valid in lane 0.
+__device__ __forceinline__ void fx_warp_sum(uint64_t& lo, uint64_t& hi) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t l2 = __shfl_down_sync(0xffffffffu, lo, off);
+    const uint64_t h2 = __shfl_down_sync(0xffffffffu, hi, off);
+    fx_add(lo, hi, l2, h2);
+  }
+}
+
+// Adds (lo, hi) to the 128-bit accumulator acc[0..1] (lo word first).
+__device__ __forceinline__ void fx_atomic_add(unsigned long long* acc, uint64_t lo, uint64_t hi) {
+  const unsigned long long old = atomicAdd(acc, (unsigned long long)lo);
+  const unsigned long long carry = (old + lo < old) ? 1ull : 0ull;
+  atomicAdd(acc + 1, (unsigned long long)(hi + carry));
+}
+
+// The accumulated value as FP64 (one rounding).
+__device__ __forceinline__ double fx_to_double(uint64_t lo, uint64_t hi) {
+  const bool neg = (int64_t)hi < 0;
+  if (neg) fx_neg(lo, hi);
+  const double d = ((double)hi * 0x1.0p64 + (double)lo) * 0x1.0p-64;
+  return neg ? -d : d;
+}
+
+}  // namespace rh

@@ -83,11 +83,15 @@ struct CellDyn {
   long long out_count;  // output records produced
   BeatTracker bt;       // per-beat statistics in progress
   long long stats_count;  // beat records produced
+  // sum cs, xicat, xinaca of the step in progress as 128-bit fixed point
+  // (value * 2^64, lo word first), added to by every CTA of the cell and
+  // read and cleared by the last one (fixedsum.cuh)
+  unsigned long long acc[6];
 };
 
-// Quantities each CTA reduces over its CRUs.  The first three are needed
-// every step (:435-456) and carry a compensation term; the rest only at
-// output steps (:839-929).
+// Quantities each CTA reduces over its CRUs at output steps (:839-929), in
+// FP64 partials per tile.  The first three slots are unused: the per-step
+// sums (:435-456) go through the fixed-point accumulators of CellDyn.
 enum PartialIdx {
   P_CS = 0,      // sum cs (new)           [sum, comp]
   P_XICAT = 2,   // sum xicat              [sum, comp]

@@ -1220,6 +1220,12 @@ int rh_kernel_timing(rh_sim* s, int64_t* launches, double* ms) {
   return RH_OK;
 }
 
+int rh_num_groups(const rh_sim* s, int32_t* groups) {
+  if (!s || !groups) return RH_ERR_ARG;
+  *groups = s->ngroups;
+  return RH_OK;
+}
+
 int rh_last_error(const rh_sim* s, char* buf, size_t n) {
   if (!buf || n == 0) return RH_ERR_ARG;
   const char* m = s ? s->err.c_str() : g_create_error.c_str();

@@ -7,20 +7,22 @@
 //      sub-voxels are staged in shared memory so that in-tile stencil
 //      neighbours (+-x always, +-y when the row above/below is in the tile)
 //      come from shared memory and only the rest from L1/L2;
-//   2. the CTA reduces sum(cs), sum(xicat), sum(xinaca) (and at output steps
-//      the ~30 statistics of :839-929) with warp shuffles, error-free in the
-//      kernel's precision and compensated in FP64, and stores one partial per
-//      tile;
-//   3. the last CTA of a cell to finish (atomic arrival counter) sums the
-//      cell's partials in a fixed order, runs the membrane model and V update
-//      (:430-739, the reference's host loop), writes the output record at
-//      output steps, and prepares the coefficients of the next step.
+//   2. the CTA reduces sum(cs), sum(xicat), sum(xinaca) exactly in 128-bit
+//      fixed point (fixedsum.cuh) and adds them to the cell's accumulators
+//      with integer atomics; at output steps it also stores the ~30
+//      statistics of :839-929 as one FP64 partial per tile;
+//   3. the last CTA of a cell to finish (atomic arrival counter) reads the
+//      sums (and sums the output partials in a fixed order), runs the
+//      membrane model and V update (:430-739, the reference's host loop)
+//      with one warp, writes the output record at output steps, and
+//      prepares the coefficients of the next step.
 // A time step is therefore one kernel launch with no host round trip.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "cellmodel.cuh"
 #include "cellwarp.cuh"
+#include "fixedsum.cuh"
 #include "lattice.cuh"
 #include "model.cuh"
 #include "step.cuh"
@@ -29,47 +31,6 @@
 namespace rh {
 
 // ---------------------------------------------------------------- reductions
-
-__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
-  s = a + b;
-  double bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
-  s = a + b;
-  float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-// Compensated warp sum of one value per lane; (sum, comp) valid in lane 0.
-__device__ __forceinline__ void warp_sum_comp(double v, double& s, double& c) {
-  s = v;
-  c = 0.0;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    double so = __shfl_down_sync(0xffffffffu, s, off);
-    double co = __shfl_down_sync(0xffffffffu, c, off);
-    double e;
-    two_sum(s, so, s, e);
-    c = c + co + e;
-  }
-}
-
-// Same for float lane values: error-free in FP32, widened to FP64 at the end.
-__device__ __forceinline__ void warp_sum_comp(float v, double& s, double& c) {
-  float fs = v, fc = 0.0f;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    float so = __shfl_down_sync(0xffffffffu, fs, off);
-    float co = __shfl_down_sync(0xffffffffu, fc, off);
-    float e;
-    two_sum_f(fs, so, fs, e);
-    fc = fc + co + e;
-  }
-  s = (double)fs;
-  c = (double)fc;
-}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -94,22 +55,11 @@ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step, doubl
   const CellConst& cc = a.cells[cell];
   const double* P = a.partials;
   const int t0 = cc.tile_begin, nt = cc.tile_count;
-  // fixed-order sums over the cell's tiles: lane l takes tiles l, l+32, ...
+  // the step's exact whole-cell sums, accumulated by the cell's CTAs
   double tot[3];
 #pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    double s = 0.0, c = 0.0;
-    for (int tl = lane; tl < nt; tl += 32) {
-      const double* p = P + (size_t)(t0 + tl) * P_COUNT + 2 * q;
-      double e;
-      two_sum(s, __ldcg(p), s, e);
-      c += e + __ldcg(p + 1);
-    }
-    double ws, wc;
-    warp_sum_comp(s, ws, wc);
-    double wc2 = warp_sum(c);
-    tot[q] = __shfl_sync(0xffffffffu, ws + (wc + wc2), 0);
-  }
+  for (int q = 0; q < 3; ++q)
+    tot[q] = fx_to_double(__ldcg(&dyn->acc[2 * q]), __ldcg(&dyn->acc[2 * q + 1]));
   double osum[NOUT];
   if (out_step) {
     for (int q = 0; q < NOUT; ++q) {
@@ -179,24 +129,37 @@ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step, doubl
 
 // Dynamic shared memory of one CTA (tile of B CRUs).  Always the z-pair
 // planes of ci and cnsr, which the stencil reads from neighbouring threads.
-// FP32 kernels also stage every other field of the tile's CRUs with
-// asynchronous copies issued at the top of the kernel, so a thread's whole
-// state arrives in one batch (the copies of the fields updated in place
-// overlap the cell-header load); the FP64 kernels are bound by the FP64
-// pipe, not by memory latency, and read those fields directly.
+// FP32 kernels also stage, with asynchronous copies issued at the top of the
+// kernel, the tile's per-CRU scalars and integers (their copies overlap the
+// cell-header load) and the stencil halo (the neighbours of the tile's CRUs
+// along y and z, and one CRU at each end along x), so the sub-voxel loop
+// reads no neighbour from global memory.  The FP64 kernels are bound by the
+// FP64 pipe, not by memory latency, and read global memory directly.
 template <class R, int B>
 struct TileSmem {
   using V = typename Vec2<R>::T;
   static constexpr bool kStage = sizeof(R) == 4;
+  // The six cytosolic buffer fields (half of the state) are read straight
+  // from global memory inside the sub-voxel loop: staging them as well costs
+  // more in resident CTAs than it saves in latency.
+  static constexpr bool kStageBuf = false;
   static constexpr size_t kPlane = sizeof(V) * B;     // one pair plane
   static constexpr size_t kCi = 0;                     // V[4][B]
   static constexpr size_t kCn = 4 * kPlane;            // V[4][B]
   static constexpr size_t kBuf = 8 * kPlane;           // V[6][4][B]: catf cats cacal casr camyo mgmyo
-  static constexpr size_t kSc = kBuf + 24 * kPlane;    // R[9][B]: cp cjsr cjsrb ancx casar casarh casarj casarhj cs
+  static constexpr size_t kSc = kBuf + (kStageBuf ? 24 : 0) * kPlane;  // R[9][B]: cp cjsr cjsrb ancx casar casarh casarj casarhj cs
   static constexpr size_t kLcc = kSc + 9 * sizeof(R) * B;  // uint2[B]
   static constexpr size_t kRyr = kLcc + 8 * B;             // u32[B]
   static constexpr size_t kWin = kRyr + 4 * B;             // u32[B]
-  static constexpr size_t kBytes = kStage ? kWin + 4 * B : kBuf;
+  // stencil halo of the tile (ci, cnsr; cs along z):
+  //   y: V[dir][j][field][B], dir 1 = +lx (pairs 0, 2), dir 0 = -lx (pairs 1, 3)
+  //   z: V[dir][pair][field][B], dir 1 = +lx*ly, 0 = -lx*ly
+  //   x: V[side][pair][field], side 0 = the CRU before the tile, 1 = after it
+  static constexpr size_t kHy = kWin + 4 * B;
+  static constexpr size_t kHz = kHy + 8 * kPlane;
+  static constexpr size_t kHcs = kHz + 16 * kPlane;        // R[dir][B]
+  static constexpr size_t kHx = kHcs + 2 * sizeof(R) * B;  // V[2][4][2]
+  static constexpr size_t kBytes = kStage ? kHx + 16 * sizeof(V) : kBuf;
 };
 
 struct TileHeader {
@@ -223,7 +186,12 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   uint2* s_lcc = reinterpret_cast<uint2*>(dsm + TS::kLcc);
   uint32_t* s_ryr = reinterpret_cast<uint32_t*>(dsm + TS::kRyr);
   uint32_t* s_win = reinterpret_cast<uint32_t*>(dsm + TS::kWin);
+  V(*s_hy)[2][2][kBlock] = reinterpret_cast<V(*)[2][2][kBlock]>(dsm + TS::kHy);
+  V(*s_hz)[4][2][kBlock] = reinterpret_cast<V(*)[4][2][kBlock]>(dsm + TS::kHz);
+  R(*s_hcs)[kBlock] = reinterpret_cast<R(*)[kBlock]>(dsm + TS::kHcs);
+  V(*s_hx)[4][2] = reinterpret_cast<V(*)[4][2]>(dsm + TS::kHx);
   __shared__ double s_red[kBlock / 32][P_COUNT];
+  __shared__ uint64_t s_fx[kBlock / 32][3][2];
   __shared__ uint32_t s_status;
   __shared__ int s_last;
 
@@ -240,7 +208,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     const int64_t S = L.stride;
     constexpr int kTpp = kBlock / 2;  // threads per pair plane
     const int c2 = tid % kTpp, h2 = tid / kTpp;
-    if (2 * c2 < cpad) {
+    if (TS::kStageBuf && 2 * c2 < cpad) {
 #pragma unroll
       for (int k = 0; k < 12; ++k) {  // 6 buffers x 4 pair planes, two planes per round
         const int f = k >> 1, pl = 2 * (k & 1) + h2;
@@ -249,8 +217,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         cp_async16(&s_buf[f][pl][2 * c2],
                    reinterpret_cast<const V*>(base) + pl * S + gt0 + 2 * c2);
       }
-      if (h2 == 0) cp_async16(&s_lcc[2 * c2], L.lcc + gt0 + 2 * c2);
     }
+    if (h2 == 0 && 2 * c2 < cpad) cp_async16(&s_lcc[2 * c2], L.lcc + gt0 + 2 * c2);
     constexpr int kTpq = kBlock / 4;  // threads per 4-byte plane
     const int c4 = tid % kTpq, h4 = tid / kTpq;
     if (4 * c4 < cpad) {
@@ -327,6 +295,31 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       }
     }
     if (4 * tid < cpad) cp_async16(&s_sc[8][4 * tid], L.cs[par] + gt0 + 4 * tid);
+    if (valid) {  // the stencil halo: each thread fetches its own CRU's outer neighbours
+      const int hx = q % lx, hy = (q / lx) % ly, hz = q / lxly;
+      const R* csp = L.cs[par];
+#pragma unroll
+      for (int f = 0; f < 2; ++f) {
+        const V* src = f ? cn2 : ci2;
+        if (hy + 1 < ly) {
+          cp_async8(&s_hy[1][0][f][tid], src + g + lx);
+          cp_async8(&s_hy[1][1][f][tid], src + 2 * S + g + lx);
+        }
+        if (hy > 0) {
+          cp_async8(&s_hy[0][0][f][tid], src + S + g - lx);
+          cp_async8(&s_hy[0][1][f][tid], src + 3 * S + g - lx);
+        }
+#pragma unroll
+        for (int pl = 0; pl < 4; ++pl) {
+          if (hz + 1 < lz) cp_async8(&s_hz[1][pl][f][tid], src + pl * S + g + lxly);
+          if (hz > 0) cp_async8(&s_hz[0][pl][f][tid], src + pl * S + g - lxly);
+          if (tid == 0 && hx > 0) cp_async8(&s_hx[0][pl][f], src + pl * S + g - 1);
+          if (tid == count - 1 && hx + 1 < lx) cp_async8(&s_hx[1][pl][f], src + pl * S + g + 1);
+        }
+      }
+      if (hz + 1 < lz) cp_async4(&s_hcs[1][tid], csp + g + lxly);
+      if (hz > 0) cp_async4(&s_hcs[0][tid], csp + g - lxly);
+    }
     cp_async_wait_all();
   } else {
 #pragma unroll
@@ -403,6 +396,16 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       const V c = s_ci2[p][tid], n = s_cn2[p][tid];
       // z
       V czp = c, nzp = n, czm = c, nzm = n;
+      if (kStage) {
+        if (has_zp) {
+          czp = s_hz[1][p][0][tid];
+          nzp = s_hz[1][p][1][tid];
+        }
+        if (has_zm) {
+          czm = s_hz[0][p][0][tid];
+          nzm = s_hz[0][p][1][tid];
+        }
+      } else {
       if (has_zp) {
         if (zp_in) {
           czp = s_ci2[p][tid + lxly];
@@ -421,6 +424,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
           nzm = __ldg(cn2 + gp - lxly);
         }
       }
+      }
       const V ciN = v2(c.y, has_zp ? czp.x : c.y), cnN = v2(n.y, has_zp ? nzp.x : n.y);
       const V ciS = v2(has_zm ? czm.y : c.x, c.x), cnS = v2(has_zm ? nzm.y : n.x, n.x);
       // y: pair p^1
@@ -431,7 +435,10 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         V ci_ex = c, cn_ex = n;
         const int d = by ? lx : -lx;
         if (by ? has_yp : has_ym) {
-          if (by ? yp_in : ym_in) {
+          if (kStage) {
+            ci_ex = s_hy[by][p >> 1][0][tid];
+            cn_ex = s_hy[by][p >> 1][1][tid];
+          } else if (by ? yp_in : ym_in) {
             ci_ex = s_ci2[py][tid + d];
             cn_ex = s_cn2[py][tid + d];
           } else {
@@ -455,6 +462,9 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
           if (bx ? xp_in : xm_in) {
             ci_ex = s_ci2[px][tid + d];
             cn_ex = s_cn2[px][tid + d];
+          } else if (kStage) {
+            ci_ex = s_hx[bx][px][0];
+            cn_ex = s_hx[bx][px][1];
           } else {
             ci_ex = __ldg(ci2 + px * S + g + d);
             cn_ex = __ldg(cn2 + px * S + g + d);
@@ -485,9 +495,10 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       }
       // cytosolic buffers (buffers.c:55-115): on*(B-b) - koff*b, with the
       // saturation guard kon*c*dt > 1 taken on the rare slow path
-      V catf = kStage ? s_buf[0][p][tid] : catf2[gp], cats = kStage ? s_buf[1][p][tid] : cats2[gp];
-      V cacal = kStage ? s_buf[2][p][tid] : cacal2[gp], casr = kStage ? s_buf[3][p][tid] : casr2[gp];
-      V camyo = kStage ? s_buf[4][p][tid] : camyo2[gp], mgmyo = kStage ? s_buf[5][p][tid] : mgmyo2[gp];
+      constexpr bool kSB = TS::kStageBuf;
+      V catf = kSB ? s_buf[0][p][tid] : catf2[gp], cats = kSB ? s_buf[1][p][tid] : cats2[gp];
+      V cacal = kSB ? s_buf[2][p][tid] : cacal2[gp], casr = kSB ? s_buf[3][p][tid] : casr2[gp];
+      V camyo = kSB ? s_buf[4][p][tid] : camyo2[gp], mgmyo = kSB ? s_buf[5][p][tid] : mgmyo2[gp];
       const V freemyo = vsub(vsub(splat2(R(BMYO)), camyo), mgmyo);
       V r_tf = vfma(vmul(splat2(R(KTFON)), c), vsub(splat2(R(BTF)), catf), vmul(splat2(R(-KTFOFF)), catf));
       V r_ts = vfma(vmul(splat2(R(KTSON)), c), vsub(splat2(R(BTS)), cats), vmul(splat2(R(-KTSOFF)), cats));
@@ -651,8 +662,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     {
       const R dth = k.dth, rdth95 = k.rdth95;
       R csN = cs0, csS = cs0;
-      if (has_zp) csN = (kStage && tid + lxly < count) ? s_sc[8][tid + lxly] : __ldg(cs + g + lxly);
-      if (has_zm) csS = (kStage && tid - lxly >= 0) ? s_sc[8][tid - lxly] : __ldg(cs + g - lxly);
+      if (has_zp) csN = kStage ? s_hcs[1][tid] : __ldg(cs + g + lxly);
+      if (has_zm) csS = kStage ? s_hcs[0][tid] : __ldg(cs + g - lxly);
       const R csdiff = (csN + csS - R(2) * cs0) * R(1.0 / TAUST);
       const R cs_const = -R(ICAGAMMA * VP / VS) * icat1 + xinaca -
                          (cs0 - ci0) * R(1.0 / TAUSI / 2.) - (cs0 - ci1) * R(1.0 / TAUSI / 2.) +
@@ -780,25 +791,23 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     }
   }
 
-  // ---- CTA reduction of the partials ----
+  // ---- CTA reduction: the per-step sums exactly (fixedsum.cuh), the
+  //      output-step statistics in FP64 partials ----
   const int warp = tid >> 5, lane = tid & 31;
   {
-    double s, c;
-    warp_sum_comp(p_cs, s, c);
-    if (lane == 0) {
-      s_red[warp][P_CS] = s;
-      s_red[warp][P_CS + 1] = c;
+    uint32_t bad = 0;
+    const R pv[3] = {p_cs, p_xicat, p_xinaca};
+#pragma unroll
+    for (int qq = 0; qq < 3; ++qq) {
+      uint64_t lo, hi;
+      fx_from(pv[qq], lo, hi, bad);
+      fx_warp_sum(lo, hi);
+      if (lane == 0) {
+        s_fx[warp][qq][0] = lo;
+        s_fx[warp][qq][1] = hi;
+      }
     }
-    warp_sum_comp(p_xicat, s, c);
-    if (lane == 0) {
-      s_red[warp][P_XICAT] = s;
-      s_red[warp][P_XICAT + 1] = c;
-    }
-    warp_sum_comp(p_xinaca, s, c);
-    if (lane == 0) {
-      s_red[warp][P_XINACA] = s;
-      s_red[warp][P_XINACA + 1] = c;
-    }
+    if (bad) atomicOr(&s_status, RH_STATUS_NAN);
     if (OUT && out_step) {
 #pragma unroll 1
       for (int kk = 0; kk < NOUT; ++kk) {
@@ -817,17 +826,12 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   if (tid < 32) {
     constexpr int NW = kBlock / 32;
     double* dst = a.partials + (size_t)(a.tile_base + blockIdx.x) * P_COUNT;
-    if (lane < 3) {
-      // compensated sum over warps in fixed order
-      double s = 0.0, c = 0.0;
+    if (lane < 3) {  // lane q adds the tile's sum q to the cell's accumulator
+      uint64_t lo = s_fx[0][lane][0], hi = s_fx[0][lane][1];
 #pragma unroll
-      for (int w = 0; w < NW; ++w) {
-        double e;
-        two_sum(s, s_red[w][2 * lane], s, e);
-        c += e + s_red[w][2 * lane + 1];
-      }
-      dst[2 * lane] = s;
-      dst[2 * lane + 1] = c;
+      for (int w = 1; w < NW; ++w) fx_add(lo, hi, s_fx[w][lane][0], s_fx[w][lane][1]);
+      fx_atomic_add(&a.dyn[cell].acc[2 * lane], lo, hi);
+      __threadfence();
     }
     if (OUT && out_step) {
       for (int kk = lane; kk < NOUT; kk += 32) {
@@ -855,6 +859,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   if (tid < 32) {
     __threadfence();
     if (!a.lattice_only) cell_update<R>(a, cell, out_step, reinterpret_cast<double*>(dsm));
+    __syncwarp();
+    if (tid < 6) a.dyn[cell].acc[tid] = 0ull;  // the next step starts from zero
     if (tid == 0) {
       a.dyn[cell].parity = par ^ 1;
       a.dyn[cell].arrive = 0;

@@ -46,6 +46,16 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
                : "memory");
 }
 
+// 8- and 4-byte variants (both addresses aligned to the size; cached in L1).
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src)
+               : "memory");
+}
+
 // Waits until every cp.async this thread issued has landed in shared memory
 // (other threads' copies need a barrier after their own wait).
 __device__ __forceinline__ void cp_async_wait_all() {

@@ -18,7 +18,7 @@ EXPORTS = [
     "rh_run_to_end", "rh_lattice_step", "rh_num_cells", "rh_cell_size", "rh_get_state",
     "rh_set_state", "rh_get_membrane", "rh_set_membrane", "rh_drain_wholecell",
     "rh_drain_linescan", "rh_drain_stats", "rh_cell_status", "rh_checkpoint", "rh_restore",
-    "rh_bytes_per_cru_step", "rh_kernel_timing", "rh_last_error", "rh_format_wholecell",
+    "rh_bytes_per_cru_step", "rh_kernel_timing", "rh_num_groups", "rh_last_error", "rh_format_wholecell",
     "rh_format_linescan", "rh_state_bytes", "rh_export_state", "rh_import_state",
     "rh_analyze_trace", "rh_autotune", "rh_tile_size",
 ]
@@ -68,6 +68,7 @@ def load() -> C.CDLL:
     L.rh_export_state.argtypes = [vp, vp, C.c_size_t]
     L.rh_import_state.argtypes = [vp, vp, C.c_size_t]
     L.rh_kernel_timing.argtypes = [vp, C.POINTER(C.c_int64), dp]
+    L.rh_num_groups.argtypes = [vp, C.POINTER(C.c_int32)]
     L.rh_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), dp]
     L.rh_tile_size.argtypes = [vp, C.POINTER(C.c_int32)]
     L.rh_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]

@@ -168,6 +168,13 @@ class Simulator:
         self._ck(self.L.rh_bytes_per_cru_step(self.h, C.byref(b)))
         return b.value
 
+    def num_groups(self) -> int:
+        """Cell groups advanced on concurrent streams (one step-kernel launch
+        per group and lattice update)."""
+        n = C.c_int32()
+        self._ck(self.L.rh_num_groups(self.h, C.byref(n)))
+        return n.value
+
     def kernel_timing(self) -> tuple[int, float]:
         n = C.c_int64()
         ms = C.c_double()
