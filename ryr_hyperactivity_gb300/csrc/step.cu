@@ -26,7 +26,7 @@
 #include "lattice.cuh"
 #include "model.cuh"
 #include "step.cuh"
-#include "tma.cuh"
+#include "async_copy.cuh"
 
 namespace rh {
 
