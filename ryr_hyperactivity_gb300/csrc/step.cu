@@ -47,9 +47,10 @@ __device__ __forceinline__ R clamp0(R x) {
 
 // Whole-cell part of the step, run by warp 0 (all 32 lanes) of the last CTA
 // of the cell.  `scratch` is 160 doubles of shared memory no longer used by
-// the tile.
+// the tile.  Not inlined: its FP64 working set would otherwise shape the
+// register allocation of the lattice code, which runs on every CTA.
 template <class R>
-__device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step, double* scratch) {
+__noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step, double* scratch) {
   const int lane = threadIdx.x & 31;
   CellDyn* dyn = a.dyn + cell;
   const CellConst& cc = a.cells[cell];
@@ -147,17 +148,26 @@ struct TileSmem {
   static constexpr size_t kCi = 0;                     // V[4][B]
   static constexpr size_t kCn = 4 * kPlane;            // V[4][B]
   static constexpr size_t kBuf = 8 * kPlane;           // V[6][4][B]: catf cats cacal casr camyo mgmyo
-  static constexpr size_t kSc = kBuf + (kStageBuf ? 24 : 0) * kPlane;  // R[9][B]: cp cjsr cjsrb ancx casar casarh casarj casarhj cs
-  static constexpr size_t kLcc = kSc + 9 * sizeof(R) * B;  // uint2[B]
-  static constexpr size_t kRyr = kLcc + 8 * B;             // u32[B]
-  static constexpr size_t kWin = kRyr + 4 * B;             // u32[B]
+  // The per-CRU scalars and integers (8 + 3 fields) are staged too when
+  // kStageSc; cs (index 8 of the scalar block) always is.
+#ifdef RH_STAGE_SC
+  static constexpr bool kStageSc = RH_STAGE_SC;
+#else
+  static constexpr bool kStageSc = kStage;
+#endif
+  static constexpr size_t kCs = kBuf + (kStageBuf ? 24 : 0) * kPlane;  // R[B]: cs
+  static constexpr size_t kSc = kCs + sizeof(R) * B;        // R[8][B]: cp cjsr cjsrb ancx casar casarh casarj casarhj
+  static constexpr size_t kLcc = kSc + (kStageSc ? 8 : 0) * sizeof(R) * B;  // uint2[B]
+  static constexpr size_t kRyr = kLcc + (kStageSc ? 8 : 0) * B;             // u32[B]
+  static constexpr size_t kWin = kRyr + (kStageSc ? 4 : 0) * B;             // u32[B]
   // stencil halo of the tile (ci, cnsr; cs along z):
   //   y: V[dir][j][field][B], dir 1 = +lx (pairs 0, 2), dir 0 = -lx (pairs 1, 3)
-  //   z: V[dir][pair][field][B], dir 1 = +lx*ly, 0 = -lx*ly
+  //   z: R[dir][pair][field][B], the pair half that faces the tile: the lower
+  //      sub-voxel of the CRU above (dir 1), the upper one of the CRU below
   //   x: V[side][pair][field], side 0 = the CRU before the tile, 1 = after it
-  static constexpr size_t kHy = kWin + 4 * B;
+  static constexpr size_t kHy = kWin + (kStageSc ? 4 : 0) * B;
   static constexpr size_t kHz = kHy + 8 * kPlane;
-  static constexpr size_t kHcs = kHz + 16 * kPlane;        // R[dir][B]
+  static constexpr size_t kHcs = kHz + 16 * sizeof(R) * B;  // R[dir][B]
   static constexpr size_t kHx = kHcs + 2 * sizeof(R) * B;  // V[2][4][2]
   static constexpr size_t kBytes = kStage ? kHx + 16 * sizeof(V) : kBuf;
 };
@@ -183,11 +193,13 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   V(*s_cn2)[kBlock] = reinterpret_cast<V(*)[kBlock]>(dsm + TS::kCn);
   V(*s_buf)[4][kBlock] = reinterpret_cast<V(*)[4][kBlock]>(dsm + TS::kBuf);
   R(*s_sc)[kBlock] = reinterpret_cast<R(*)[kBlock]>(dsm + TS::kSc);
+  R* s_cs = reinterpret_cast<R*>(dsm + TS::kCs);
+  constexpr bool kSS = TS::kStageSc;
   uint2* s_lcc = reinterpret_cast<uint2*>(dsm + TS::kLcc);
   uint32_t* s_ryr = reinterpret_cast<uint32_t*>(dsm + TS::kRyr);
   uint32_t* s_win = reinterpret_cast<uint32_t*>(dsm + TS::kWin);
   V(*s_hy)[2][2][kBlock] = reinterpret_cast<V(*)[2][2][kBlock]>(dsm + TS::kHy);
-  V(*s_hz)[4][2][kBlock] = reinterpret_cast<V(*)[4][2][kBlock]>(dsm + TS::kHz);
+  R(*s_hz)[4][2][kBlock] = reinterpret_cast<R(*)[4][2][kBlock]>(dsm + TS::kHz);
   R(*s_hcs)[kBlock] = reinterpret_cast<R(*)[kBlock]>(dsm + TS::kHcs);
   V(*s_hx)[4][2] = reinterpret_cast<V(*)[4][2]>(dsm + TS::kHx);
   __shared__ double s_red[kBlock / 32][P_COUNT];
@@ -218,10 +230,10 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
                    reinterpret_cast<const V*>(base) + pl * S + gt0 + 2 * c2);
       }
     }
-    if (h2 == 0 && 2 * c2 < cpad) cp_async16(&s_lcc[2 * c2], L.lcc + gt0 + 2 * c2);
+    if (kSS && h2 == 0 && 2 * c2 < cpad) cp_async16(&s_lcc[2 * c2], L.lcc + gt0 + 2 * c2);
     constexpr int kTpq = kBlock / 4;  // threads per 4-byte plane
     const int c4 = tid % kTpq, h4 = tid / kTpq;
-    if (4 * c4 < cpad) {
+    if (kSS && 4 * c4 < cpad) {
 #pragma unroll
       for (int f = 0; f < 10; ++f) {  // cp cjsr cjsrb ancx casar casarh casarj casarhj ryr win
         if ((f & 3) != h4) continue;
@@ -294,7 +306,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         cp_async16(&dst[pl][2 * c2], src + pl * S + gt0 + 2 * c2);
       }
     }
-    if (4 * tid < cpad) cp_async16(&s_sc[8][4 * tid], L.cs[par] + gt0 + 4 * tid);
+    if (4 * tid < cpad) cp_async16(&s_cs[4 * tid], L.cs[par] + gt0 + 4 * tid);
     if (valid) {  // the stencil halo: each thread fetches its own CRU's outer neighbours
       const int hx = q % lx, hy = (q / lx) % ly, hz = q / lxly;
       const R* csp = L.cs[par];
@@ -311,8 +323,10 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         }
 #pragma unroll
         for (int pl = 0; pl < 4; ++pl) {
-          if (hz + 1 < lz) cp_async8(&s_hz[1][pl][f][tid], src + pl * S + g + lxly);
-          if (hz > 0) cp_async8(&s_hz[0][pl][f][tid], src + pl * S + g - lxly);
+          if (hz + 1 < lz)
+            cp_async4(&s_hz[1][pl][f][tid], reinterpret_cast<const R*>(src + pl * S + g + lxly));
+          if (hz > 0)
+            cp_async4(&s_hz[0][pl][f][tid], reinterpret_cast<const R*>(src + pl * S + g - lxly) + 1);
           if (tid == 0 && hx > 0) cp_async8(&s_hx[0][pl][f], src + pl * S + g - 1);
           if (tid == count - 1 && hx + 1 < lx) cp_async8(&s_hx[1][pl][f], src + pl * S + g + 1);
         }
@@ -346,8 +360,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     V* cnnext2 = reinterpret_cast<V*>(L.cnsr[par ^ 1]);
     R* csnext = L.cs[par ^ 1];
 
-    R cp = kStage ? s_sc[0][tid] : L.cp[g], cjsr = kStage ? s_sc[1][tid] : L.cjsr[g];
-    const R cs0 = kStage ? s_sc[8][tid] : cs[g];
+    R cp = kSS ? s_sc[0][tid] : L.cp[g], cjsr = kSS ? s_sc[1][tid] : L.cjsr[g];
+    const R cs0 = kStage ? s_cs[tid] : cs[g];
     // ---- dyad/submembrane/JSR coupling terms from the old state (:1309-1314) ----
     const R ci0 = s_ci2[0][tid].x, ci1 = s_ci2[0][tid].y;
     const R cn0 = s_cn2[0][tid].x, cn1 = s_cn2[0][tid].y;
@@ -398,12 +412,12 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       V czp = c, nzp = n, czm = c, nzm = n;
       if (kStage) {
         if (has_zp) {
-          czp = s_hz[1][p][0][tid];
-          nzp = s_hz[1][p][1][tid];
+          czp.x = s_hz[1][p][0][tid];
+          nzp.x = s_hz[1][p][1][tid];
         }
         if (has_zm) {
-          czm = s_hz[0][p][0][tid];
-          nzm = s_hz[0][p][1][tid];
+          czm.y = s_hz[0][p][0][tid];
+          nzm.y = s_hz[0][p][1][tid];
         }
       } else {
       if (has_zp) {
@@ -577,10 +591,10 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     }
 
     // ---- CRU state of the stochastic part ----
-    R cjsrb = kStage ? s_sc[2][tid] : L.cjsrb[g], ancx = kStage ? s_sc[3][tid] : L.ancx[g];
-    const uint32_t ryr = kStage ? s_ryr[tid] : L.ryr[g];
-    uint2 lccw = kStage ? s_lcc[tid] : L.lcc[g];
-    const uint32_t win = kStage ? s_win[tid] : L.win[g];
+    R cjsrb = kSS ? s_sc[2][tid] : L.cjsrb[g], ancx = kSS ? s_sc[3][tid] : L.ancx[g];
+    const uint32_t ryr = kSS ? s_ryr[tid] : L.ryr[g];
+    uint2 lccw = kSS ? s_lcc[tid] : L.lcc[g];
+    const uint32_t win = kSS ? s_win[tid] : L.win[g];
     int nou = ryr & 0xff, ncu = (ryr >> 8) & 0xff, nob = (ryr >> 16) & 0xff, ncb = ryr >> 24;
     int nl = win & 0xffff, nspark = win >> 16;
     if (k.reset_window) {  // :1244-1247
@@ -656,8 +670,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     cjsrb += (R(1) - beta) * jterm * dt;
 
     // ---- five sub-steps of cs, cp and the sarcolemmal buffers (:1396-1473) ----
-    R casar = kStage ? s_sc[4][tid] : L.casar[g], casarh = kStage ? s_sc[5][tid] : L.casarh[g];
-    R casarj = kStage ? s_sc[6][tid] : L.casarj[g], casarhj = kStage ? s_sc[7][tid] : L.casarhj[g];
+    R casar = kSS ? s_sc[4][tid] : L.casar[g], casarh = kSS ? s_sc[5][tid] : L.casarh[g];
+    R casarj = kSS ? s_sc[6][tid] : L.casarj[g], casarhj = kSS ? s_sc[7][tid] : L.casarhj[g];
     R csn = cs0;
     {
       const R dth = k.dth, rdth95 = k.rdth95;
