@@ -243,12 +243,45 @@ def _cmd_screen(a):
     pred_te = model.predict(normalise(pts[te]))
     sweep = LO + (HI - LO) * rng.random((a.sweep, 4))
     flagged, holdout, _ = screen(model, sweep, a.threshold, 0.02, a.seed)
-    res = {"train_loss": losses[-1], "test_points": int(len(te)),
+    res = {"train_points": int(ntr), "train_loss": losses[-1], "test_points": int(len(te)),
            "test_ead_mae": float(np.mean(np.abs(pred_te[:, 0] - stats[te, 0]))),
            "test_apd_mae_ms": float(np.mean(np.abs(pred_te[:, 1] * APD_SCALE - stats[te, 1]))),
            "sweep": a.sweep, "flagged": int(len(flagged)), "holdout": int(len(holdout)),
            "full_model_fraction": float((len(flagged) + len(holdout)) / a.sweep)}
+    if a.verify > 0:
+        res.update(verify(model, sweep, flagged, holdout, a.verify, a.threshold, d, rng))
     print(json.dumps(res))
+
+
+def verify(model: Surrogate, sweep, flagged, holdout, cap: int, threshold: float, data, rng):
+    """Re-runs up to `cap` flagged points and `cap` holdout points with the
+    full stochastic model (the training data's lattice, duration and cells per
+    point) and reports what the surrogate got right: the fraction of flagged
+    points that do show EADs, the fraction of holdout (unflagged) points that
+    show EADs the screen missed, and the prediction errors."""
+    fl = rng.choice(flagged, min(cap, len(flagged)), replace=False) if len(flagged) else flagged
+    ho = rng.choice(holdout, min(cap, len(holdout)), replace=False) if len(holdout) else holdout
+    idx = np.concatenate([fl, ho]).astype(int)
+    t0 = time.time()
+    full = simulate_points(sweep[idx], int(data["cells_per_point"]), float(data["duration_ms"]),
+                           tuple(int(x) for x in data["lattice"]), str(data["precision"]),
+                           philox_seed=11)
+    pred = model.predict(normalise(sweep[idx]))
+    ok = full[:, 3] > 0
+    ead_true = full[:, 0] > 0
+    nf = len(fl)
+    return {
+        "verify_seconds": time.time() - t0,
+        "verified_flagged": int(nf), "verified_holdout": int(len(ho)),
+        "flagged_with_ead": float(np.mean(ead_true[:nf][ok[:nf]])) if np.any(ok[:nf]) else None,
+        "holdout_with_ead": float(np.mean(ead_true[nf:][ok[nf:]])) if np.any(ok[nf:]) else None,
+        "sweep_ead_points_est": None if not np.any(ok[nf:]) or not np.any(ok[:nf]) else float(
+            len(flagged) * np.mean(ead_true[:nf][ok[:nf]]) +
+            (len(sweep) - len(flagged)) * np.mean(ead_true[nf:][ok[nf:]])),
+        "verify_ead_prob_mae": float(np.mean(np.abs(pred[ok, 0] - full[ok, 0]))),
+        "verify_apd_mae_ms": float(np.mean(np.abs(pred[ok, 1] * APD_SCALE - full[ok, 1]))),
+        "threshold": threshold,
+    }
 
 
 def main(argv=None):
@@ -268,6 +301,8 @@ def main(argv=None):
     s.add_argument("--threshold", type=float, default=0.1)
     s.add_argument("--epochs", type=int, default=400)
     s.add_argument("--seed", type=int, default=0)
+    s.add_argument("--verify", type=int, default=0,
+                   help="re-run up to this many flagged and holdout points with the full model")
     a = ap.parse_args(argv)
     {"generate": _cmd_generate, "screen": _cmd_screen}[a.cmd](a)
 
