@@ -471,7 +471,7 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
       nt += cc.tile_count;
     }
     t.ntiles = nt;
-    max_tiles = std::max(max_tiles, nt);
+    max_tiles = std::max(max_tiles, nt * (t.tile / 32));  // partial rows: one per warp
   }
   {
     int want = s->opts.block_size > 0 ? s->opts.block_size : kDefaultTile;

@@ -50,12 +50,14 @@ __device__ __forceinline__ R clamp0(R x) {
 // the tile.  Not inlined: its FP64 working set would otherwise shape the
 // register allocation of the lattice code, which runs on every CTA.
 template <class R>
-__noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step, double* scratch) {
+__noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step, double* scratch,
+                                         int nw) {
   const int lane = threadIdx.x & 31;
   CellDyn* dyn = a.dyn + cell;
   const CellConst& cc = a.cells[cell];
   const double* P = a.partials;
-  const int t0 = cc.tile_begin, nt = cc.tile_count;
+  // output-step partials: one row per warp of each of the cell's tiles
+  const int t0 = cc.tile_begin * nw, nt = cc.tile_count * nw;
   // the step's exact whole-cell sums, accumulated by the cell's CTAs
   double tot[3];
 #pragma unroll
@@ -202,10 +204,9 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   R(*s_hz)[4][2][kBlock] = reinterpret_cast<R(*)[4][2][kBlock]>(dsm + TS::kHz);
   R(*s_hcs)[kBlock] = reinterpret_cast<R(*)[kBlock]>(dsm + TS::kHcs);
   V(*s_hx)[4][2] = reinterpret_cast<V(*)[4][2]>(dsm + TS::kHx);
-  __shared__ double s_red[kBlock / 32][P_COUNT];
-  __shared__ uint64_t s_fx[kBlock / 32][3][2];
-  __shared__ uint32_t s_status;
-  __shared__ int s_last;
+  // scratch of the cell update (run by the cell's last warp while other
+  // warps of the CTA may still be using the tile)
+  __shared__ double s_cu[160];
 
   const int4 tile = a.tiles[blockIdx.x];
   const int cell = tile.x;
@@ -271,7 +272,6 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       sh.slot = d->out_count % a.out_cap;
       sh.parity = d->parity;
       sh.done = d->done;
-      s_status = 0;
     }
   }
   __syncthreads();
@@ -345,6 +345,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   __syncthreads();
 
   R p_cs = R(0), p_xicat = R(0), p_xinaca = R(0);
+  uint32_t tstat = 0;  // this thread's status bits
   double o[OUT ? NOUT : 1];
   if (OUT) {
 #pragma unroll
@@ -725,7 +726,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       a.diag[(int64_t)D_XINACA * S + g] = (double)xinaca;
       a.diag[(int64_t)D_XICAT * S + g] = (double)icat1;
     }
-    if (status) atomicOr(&s_status, status);
+    tstat = status;
 
     p_cs = csn;
     p_xicat = icat1;
@@ -805,80 +806,63 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     }
   }
 
-  // ---- CTA reduction: the per-step sums exactly (fixedsum.cuh), the
-  //      output-step statistics in FP64 partials ----
+  // ---- per-warp reduction and arrival: the per-step sums exactly
+  //      (fixedsum.cuh) into the cell's accumulators, the output-step
+  //      statistics as one FP64 partial row per warp; no CTA barrier ----
   const int warp = tid >> 5, lane = tid & 31;
+  constexpr int NW = kBlock / 32;
+  uint64_t qlo = 0, qhi = 0;  // lane q < 3: the warp's sum q
+  uint32_t bad = 0;
   {
-    uint32_t bad = 0;
     const R pv[3] = {p_cs, p_xicat, p_xinaca};
 #pragma unroll
     for (int qq = 0; qq < 3; ++qq) {
       uint64_t lo, hi;
       fx_from(pv[qq], lo, hi, bad);
       fx_warp_sum(lo, hi);
-      if (lane == 0) {
-        s_fx[warp][qq][0] = lo;
-        s_fx[warp][qq][1] = hi;
+      lo = __shfl_sync(0xffffffffu, lo, 0);
+      hi = __shfl_sync(0xffffffffu, hi, 0);
+      if (lane == qq) {
+        qlo = lo;
+        qhi = hi;
       }
     }
-    if (bad) atomicOr(&s_status, RH_STATUS_NAN);
-    if (OUT && out_step) {
+  }
+  const uint32_t wst = __reduce_or_sync(0xffffffffu, tstat | (bad ? (uint32_t)RH_STATUS_NAN : 0u));
+  if (OUT && out_step) {
+    double* dst = a.partials + ((size_t)(a.tile_base + blockIdx.x) * NW + warp) * P_COUNT;
 #pragma unroll 1
-      for (int kk = 0; kk < NOUT; ++kk) {
-        double v = o[kk];
-        if (kk == O_CIHIGH - P_STEP_END) {
+    for (int kk = 0; kk < NOUT; ++kk) {
+      double v = o[kk];
+      if (kk == O_CIHIGH - P_STEP_END) {
 #pragma unroll
-          for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
-        } else {
-          v = warp_sum(v);
-        }
-        if (lane == 0) s_red[warp][P_STEP_END + kk] = v;
+        for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+      } else {
+        v = warp_sum(v);
       }
+      if (lane == 0) dst[P_STEP_END + kk] = v;
     }
   }
-  __syncthreads();
-  if (tid < 32) {
-    constexpr int NW = kBlock / 32;
-    double* dst = a.partials + (size_t)(a.tile_base + blockIdx.x) * P_COUNT;
-    if (lane < 3) {  // lane q adds the tile's sum q to the cell's accumulator
-      uint64_t lo = s_fx[0][lane][0], hi = s_fx[0][lane][1];
-#pragma unroll
-      for (int w = 1; w < NW; ++w) fx_add(lo, hi, s_fx[w][lane][0], s_fx[w][lane][1]);
-      fx_atomic_add(&a.dyn[cell].acc[2 * lane], lo, hi);
-      __threadfence();
-    }
-    if (OUT && out_step) {
-      for (int kk = lane; kk < NOUT; kk += 32) {
-        double v = 0.0;
-        if (kk == O_CIHIGH - P_STEP_END) {
-          for (int w = 0; w < NW; ++w) v = fmax(v, s_red[w][P_STEP_END + kk]);
-        } else {
-          for (int w = 0; w < NW; ++w) v += s_red[w][P_STEP_END + kk];
-        }
-        dst[P_STEP_END + kk] = v;
-      }
-    }
-    __syncwarp();
-    if (lane == 0) {
-      if (s_status) atomicOr(&a.dyn[cell].status, s_status);
-      __threadfence();
-      unsigned int prev = atomicAdd(&a.dyn[cell].arrive, 1u);
-      s_last = (prev == (unsigned)(sh.tile_count - 1));
-    }
-    __syncwarp();
+  if (lane < 3) {
+    fx_atomic_add(&a.dyn[cell].acc[2 * lane], qlo, qhi);
+    if (lane == 0 && wst) atomicOr(&a.dyn[cell].status, wst);
+    __threadfence();  // the adds (and the output partials) before the arrival
   }
-  __syncthreads();
-  if (!s_last) return;
-  // ---- last CTA of the cell: whole-cell update ----
-  if (tid < 32) {
-    __threadfence();
-    if (!a.lattice_only) cell_update<R>(a, cell, out_step, reinterpret_cast<double*>(dsm));
-    __syncwarp();
-    if (tid < 6) a.dyn[cell].acc[tid] = 0ull;  // the next step starts from zero
-    if (tid == 0) {
-      a.dyn[cell].parity = par ^ 1;
-      a.dyn[cell].arrive = 0;
-    }
+  __syncwarp();
+  int last = 0;
+  if (lane == 0) {
+    const unsigned int prev = atomicAdd(&a.dyn[cell].arrive, 1u);
+    last = prev == (unsigned)(sh.tile_count * NW - 1);
+  }
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  // ---- last warp of the cell: whole-cell update ----
+  __threadfence();
+  if (!a.lattice_only) cell_update<R>(a, cell, out_step, s_cu, NW);
+  __syncwarp();
+  if (lane < 6) a.dyn[cell].acc[lane] = 0ull;  // the next step starts from zero
+  if (lane == 0) {
+    a.dyn[cell].parity = par ^ 1;
+    a.dyn[cell].arrive = 0;
   }
 }
 
