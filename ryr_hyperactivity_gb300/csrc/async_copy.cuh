@@ -28,6 +28,17 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src) {
                : "memory");
 }
 
+// Closes the group of this thread's cp.async copies issued since the last
+// commit; cp_async_wait_group<N> waits until at most N of its groups are
+// still in flight (again only this thread's copies).
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // Waits until every cp.async this thread issued has landed in shared memory
 // (other threads' copies need a barrier after their own wait).
 __device__ __forceinline__ void cp_async_wait_all() {

@@ -307,9 +307,14 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       }
     }
     if (4 * tid < cpad) cp_async16(&s_cs[4 * tid], L.cs[par] + gt0 + 4 * tid);
-    if (valid) {  // the stencil halo: each thread fetches its own CRU's outer neighbours
-      const int hx = q % lx, hy = (q / lx) % ly, hz = q / lxly;
+    const int hx = q % lx, hy = (q / lx) % ly, hz = q / lxly;
+    if (valid) {  // cs of the z-neighbours (the sub-steps need it first)
       const R* csp = L.cs[par];
+      if (hz + 1 < lz) cp_async4(&s_hcs[1][tid], csp + g + lxly);
+      if (hz > 0) cp_async4(&s_hcs[0][tid], csp + g - lxly);
+    }
+    cp_async_commit();  // group 1: everything the channel part reads
+    if (valid) {  // the stencil halo: each thread fetches its own CRU's outer neighbours
 #pragma unroll
       for (int f = 0; f < 2; ++f) {
         const V* src = f ? cn2 : ci2;
@@ -331,10 +336,9 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
           if (tid == count - 1 && hx + 1 < lx) cp_async8(&s_hx[1][pl][f], src + pl * S + g + 1);
         }
       }
-      if (hz + 1 < lz) cp_async4(&s_hcs[1][tid], csp + g + lxly);
-      if (hz > 0) cp_async4(&s_hcs[0][tid], csp + g - lxly);
     }
-    cp_async_wait_all();
+    cp_async_commit();       // group 2: the halo, which only its own thread reads
+    cp_async_wait_group<1>();  // group 1 has landed (this thread's part of it)
   } else {
 #pragma unroll
     for (int p = 0; p < 4; ++p) {
@@ -373,223 +377,20 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     const R diffjn0 = (cjsr - cn0) * R(1.0 / TAUTR / 2.);
     const R diffjn1 = (cjsr - cn1) * R(1.0 / TAUTR / 2.);
 
-    // ---- sub-voxel diffusion, SERCA/leak, cytosolic buffers (:1305-1393) ----
-    // Processed as four z-pairs p = (sub-voxels 2p, 2p+1).  Along z the pair's
-    // halves are each other's neighbour; the outer neighbours are the
-    // adjacent CRUs' pair p.  Along y (x) the neighbour pair is p^1 (p^2) of
-    // this CRU or of the adjacent CRU in the direction of the pair's y (x)
-    // bit.  At a lattice face the zero-flux ghost equals the sub-voxel
-    // itself (:1601-1652), so that difference vanishes.
     const bool has_zp = z + 1 < lz, has_zm = z > 0;
-    const bool has_yp = y + 1 < ly, has_ym = y > 0;
-    const bool has_xp = x + 1 < lx, has_xm = x > 0;
-    const bool zp_in = tid + lxly < count, zm_in = tid - lxly >= 0;
-    const bool yp_in = tid + lx < count, ym_in = tid - lx >= 0;
-    const bool xp_in = tid + 1 < count, xm_in = tid - 1 >= 0;
-    const V kt_n = splat2(R(1.0 / (TAUNT * XI))), kl_n = splat2(R(1.0 / (TAUNL * XI)));
-    const V kt_i = splat2(R(1.0 / (TAUIT * XI))), kl_i = splat2(R(1.0 / (TAUIL * XI)));
-    const V dt2 = splat2(dt);
-    const V* catf2 = reinterpret_cast<const V*>(L.catf);
-    const V* cats2 = reinterpret_cast<const V*>(L.cats);
-    const V* cacal2 = reinterpret_cast<const V*>(L.cacal);
-    const V* casr2 = reinterpret_cast<const V*>(L.casr);
-    const V* camyo2 = reinterpret_cast<const V*>(L.camyo);
-    const V* mgmyo2 = reinterpret_cast<const V*>(L.mgmyo);
-    V* catf2w = reinterpret_cast<V*>(L.catf);
-    V* cats2w = reinterpret_cast<V*>(L.cats);
-    V* cacal2w = reinterpret_cast<V*>(L.cacal);
-    V* casr2w = reinterpret_cast<V*>(L.casr);
-    V* camyo2w = reinterpret_cast<V*>(L.camyo);
-    V* mgmyo2w = reinterpret_cast<V*>(L.mgmyo);
-    R sum_ci = R(0), sum_cn = R(0), sum_catf = R(0), sum_cats = R(0), sum_casr = R(0);
-    R sum_camyo = R(0), sum_cacal = R(0), sum_up = R(0), sum_lk = R(0);
-    bool ci_high = false;
-#pragma unroll 1
-    for (int p = 0; p < 4; ++p) {
-      const int by = p & 1, bx = p >> 1;
-      const int64_t gp = p * S + g;
-      const V c = s_ci2[p][tid], n = s_cn2[p][tid];
-      // z
-      V czp = c, nzp = n, czm = c, nzm = n;
-      if (kStage) {
-        if (has_zp) {
-          czp.x = s_hz[1][p][0][tid];
-          nzp.x = s_hz[1][p][1][tid];
-        }
-        if (has_zm) {
-          czm.y = s_hz[0][p][0][tid];
-          nzm.y = s_hz[0][p][1][tid];
-        }
-      } else {
-      if (has_zp) {
-        if (zp_in) {
-          czp = s_ci2[p][tid + lxly];
-          nzp = s_cn2[p][tid + lxly];
-        } else {
-          czp = __ldg(ci2 + gp + lxly);
-          nzp = __ldg(cn2 + gp + lxly);
-        }
-      }
-      if (has_zm) {
-        if (zm_in) {
-          czm = s_ci2[p][tid - lxly];
-          nzm = s_cn2[p][tid - lxly];
-        } else {
-          czm = __ldg(ci2 + gp - lxly);
-          nzm = __ldg(cn2 + gp - lxly);
-        }
-      }
-      }
-      const V ciN = v2(c.y, has_zp ? czp.x : c.y), cnN = v2(n.y, has_zp ? nzp.x : n.y);
-      const V ciS = v2(has_zm ? czm.y : c.x, c.x), cnS = v2(has_zm ? nzm.y : n.x, n.x);
-      // y: pair p^1
-      V ciE, cnE, ciW, cnW;
-      {
-        const int py = p ^ 1;
-        const V ci_in = s_ci2[py][tid], cn_in = s_cn2[py][tid];
-        V ci_ex = c, cn_ex = n;
-        const int d = by ? lx : -lx;
-        if (by ? has_yp : has_ym) {
-          if (kStage) {
-            ci_ex = s_hy[by][p >> 1][0][tid];
-            cn_ex = s_hy[by][p >> 1][1][tid];
-          } else if (by ? yp_in : ym_in) {
-            ci_ex = s_ci2[py][tid + d];
-            cn_ex = s_cn2[py][tid + d];
-          } else {
-            ci_ex = __ldg(ci2 + py * S + g + d);
-            cn_ex = __ldg(cn2 + py * S + g + d);
-          }
-        }
-        ciE = by ? ci_ex : ci_in;
-        cnE = by ? cn_ex : cn_in;
-        ciW = by ? ci_in : ci_ex;
-        cnW = by ? cn_in : cn_ex;
-      }
-      // x: pair p^2
-      V ciT, cnT, ciB, cnB;
-      {
-        const int px = p ^ 2;
-        const V ci_in = s_ci2[px][tid], cn_in = s_cn2[px][tid];
-        V ci_ex = c, cn_ex = n;
-        const int d = bx ? 1 : -1;
-        if (bx ? has_xp : has_xm) {
-          if (bx ? xp_in : xm_in) {
-            ci_ex = s_ci2[px][tid + d];
-            cn_ex = s_cn2[px][tid + d];
-          } else if (kStage) {
-            ci_ex = s_hx[bx][px][0];
-            cn_ex = s_hx[bx][px][1];
-          } else {
-            ci_ex = __ldg(ci2 + px * S + g + d);
-            cn_ex = __ldg(cn2 + px * S + g + d);
-          }
-        }
-        ciT = bx ? ci_ex : ci_in;
-        cnT = bx ? cn_ex : cn_in;
-        ciB = bx ? ci_in : ci_ex;
-        cnB = bx ? cn_in : cn_ex;
-      }
-      const V coupn = vfma(vadd(vadd(vadd(vsub(cnN, n), vsub(cnS, n)), vsub(cnE, n)), vsub(cnW, n)),
-                           kt_n, vmul(vadd(vsub(cnT, n), vsub(cnB, n)), kl_n));
-      const V coupi = vfma(vadd(vadd(vadd(vsub(ciN, c), vsub(ciS, c)), vsub(ciE, c)), vsub(ciW, c)),
-                           kt_i, vmul(vadd(vsub(ciT, c), vsub(ciB, c)), kl_i));
-      // SERCA and leak (subroutine_cuda.c:128-146)
-      V up, lk;
-      {
-        const R pax = Math<R>::powpos(c.x * R(1.0 / KI_UP), R(HH_UP));
-        const R pay = Math<R>::powpos(c.y * R(1.0 / KI_UP), R(HH_UP));
-        const R pbx = Math<R>::powpos(n.x * R(1.0 / KNSR_UP), R(HH_UP));
-        const R pby = Math<R>::powpos(n.y * R(1.0 / KNSR_UP), R(HH_UP));
-        up = v2(k.sviup * Math<R>::div(R(VUP) * (pax - pbx), R(1) + pax + pbx),
-                k.sviup * Math<R>::div(R(VUP) * (pay - pby), R(1) + pay + pby));
-        const V n2 = vmul(n, n);
-        const V num = vmul(vmul(splat2(R(GLEAK)), vsub(n, c)), n2);
-        const V den = vadd(n2, splat2(R(KJSR_LEAK * KJSR_LEAK)));
-        lk = v2(Math<R>::div(num.x, den.x), Math<R>::div(num.y, den.y));
-      }
-      // cytosolic buffers (buffers.c:55-115): on*(B-b) - koff*b, with the
-      // saturation guard kon*c*dt > 1 taken on the rare slow path
-      constexpr bool kSB = TS::kStageBuf;
-      V catf = kSB ? s_buf[0][p][tid] : catf2[gp], cats = kSB ? s_buf[1][p][tid] : cats2[gp];
-      V cacal = kSB ? s_buf[2][p][tid] : cacal2[gp], casr = kSB ? s_buf[3][p][tid] : casr2[gp];
-      V camyo = kSB ? s_buf[4][p][tid] : camyo2[gp], mgmyo = kSB ? s_buf[5][p][tid] : mgmyo2[gp];
-      const V freemyo = vsub(vsub(splat2(R(BMYO)), camyo), mgmyo);
-      V r_tf = vfma(vmul(splat2(R(KTFON)), c), vsub(splat2(R(BTF)), catf), vmul(splat2(R(-KTFOFF)), catf));
-      V r_ts = vfma(vmul(splat2(R(KTSON)), c), vsub(splat2(R(BTS)), cats), vmul(splat2(R(-KTSOFF)), cats));
-      V r_cal = vfma(vmul(splat2(R(KCALON)), c), vsub(splat2(R(BCAL)), cacal),
-                     vmul(splat2(R(-KCALOFF)), cacal));
-      V r_sr = vfma(vmul(splat2(R(KSRON)), c), vsub(splat2(R(BSR)), casr), vmul(splat2(R(-KSROFF)), casr));
-      V r_mc = vfma(vmul(splat2(R(KONMYOCA)), c), freemyo, vmul(splat2(R(-KOFFMYOCA)), camyo));
-      if (fmax(c.x, c.y) * R(KONMYOCA) * dt > R(1)) {  // some buffer saturates
-        const R cc[2] = {c.x, c.y};
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const R cv = cc[h];
-          R& tf = h ? r_tf.y : r_tf.x;
-          R& ts = h ? r_ts.y : r_ts.x;
-          R& cal = h ? r_cal.y : r_cal.x;
-          R& sr = h ? r_sr.y : r_sr.x;
-          R& mc = h ? r_mc.y : r_mc.x;
-          tf = buffer_rate<R>(R(KTFON), R(KTFOFF), R(BTF), h ? catf.y : catf.x, cv, dt, k.rdt95);
-          ts = buffer_rate<R>(R(KTSON), R(KTSOFF), R(BTS), h ? cats.y : cats.x, cv, dt, k.rdt95);
-          cal = buffer_rate<R>(R(KCALON), R(KCALOFF), R(BCAL), h ? cacal.y : cacal.x, cv, dt, k.rdt95);
-          sr = buffer_rate<R>(R(KSRON), R(KSROFF), R(BSR), h ? casr.y : casr.x, cv, dt, k.rdt95);
-          const R fmy = h ? freemyo.y : freemyo.x;
-          const R cm = h ? camyo.y : camyo.x;
-          const R onmc = R(KONMYOCA) * cv;
-          mc = (onmc * dt > R(1)) ? k.rdt95 * fmy - R(KOFFMYOCA) * cm : onmc * fmy - R(KOFFMYOCA) * cm;
-        }
-      }
-      V dotcn = vfma(vsub(up, lk), splat2(R(VI / VNSR)), coupn);
-      V dotci = vadd(vsub(vsub(lk, up), vadd(vadd(vadd(vadd(r_tf, r_ts), r_cal), r_sr), r_mc)), coupi);
-      if (p == 0) {  // sub-voxels 0 and 1 touch the dyad, submembrane and JSR (:1356-1361)
-        dotcn = vfma(v2(diffjn0, diffjn1), splat2(R(VJSR / VNSR)), dotcn);
-        dotci = vfma(v2(diffsi0, diffsi1), splat2(R(VS / VI)), dotci);
-        dotci = vfma(v2(diffpi0, diffpi1), splat2(R(VP / VI)), dotci);
-      }
-      const V cinew = vclamp0(vfma(dotci, dt2, c));
-      const V cnnew = vfma(dotcn, dt2, n);
-      catf = vclamp0(vfma(r_tf, dt2, catf));
-      cats = vclamp0(vfma(r_ts, dt2, cats));
-      cacal = vclamp0(vfma(r_cal, dt2, cacal));
-      casr = vclamp0(vfma(r_sr, dt2, casr));
-      camyo = vclamp0(vfma(r_mc, dt2, camyo));
-      {
-        const V fm = vsub(vsub(splat2(R(BMYO)), camyo), mgmyo);
-        V r_mg = vfma(splat2(R(KONMYOMG * MGI)), fm, vmul(splat2(R(-KOFFMYOMG)), mgmyo));
-        if (R(KONMYOMG * MGI) * dt > R(1)) {  // guard of myomg (buffers.c:65)
-          r_mg = vfma(splat2(k.rdt95), fm, vmul(splat2(R(-KOFFMYOMG)), mgmyo));
-        }
-        mgmyo = vclamp0(vfma(r_mg, dt2, mgmyo));
-      }
-      cinext2[gp] = cinew;
-      cnnext2[gp] = cnnew;
-      catf2w[gp] = catf;
-      cats2w[gp] = cats;
-      cacal2w[gp] = cacal;
-      casr2w[gp] = casr;
-      camyo2w[gp] = camyo;
-      mgmyo2w[gp] = mgmyo;
-      if (a.diag) {
-        a.diag[(int64_t)(D_XIUP + 2 * p) * S + g] = (double)up.x;
-        a.diag[(int64_t)(D_XIUP + 2 * p + 1) * S + g] = (double)up.y;
-        a.diag[(int64_t)(D_XILEAK + 2 * p) * S + g] = (double)lk.x;
-        a.diag[(int64_t)(D_XILEAK + 2 * p + 1) * S + g] = (double)lk.y;
-      }
-      if (OUT && out_step) {
-        sum_ci += cinew.x + cinew.y;
-        sum_cn += cnnew.x + cnnew.y;
-        sum_catf += catf.x + catf.y;
-        sum_cats += cats.x + cats.y;
-        sum_casr += casr.x + casr.y;
-        sum_camyo += camyo.x + camyo.y;
-        sum_cacal += cacal.x + cacal.y;
-        sum_up += up.x + up.y;
-        sum_lk += lk.x + lk.y;
-        ci_high |= (cinew.x > R(1000)) || (cinew.y > R(1000));
-      }
+    // the buffer fields of pair p + 1 load while pair p is computed (those
+    // of pair 0 while the channel part runs)
+    V nb0, nb1, nb2, nb3, nb4, nb5;
+    if (!TS::kStageBuf) {
+      const V* b2 = reinterpret_cast<const V*>(L.catf);
+      nb0 = b2[g];
+      nb1 = reinterpret_cast<const V*>(L.cats)[g];
+      nb2 = reinterpret_cast<const V*>(L.cacal)[g];
+      nb3 = reinterpret_cast<const V*>(L.casr)[g];
+      nb4 = reinterpret_cast<const V*>(L.camyo)[g];
+      nb5 = reinterpret_cast<const V*>(L.mgmyo)[g];
     }
+
 
     // ---- CRU state of the stochastic part ----
     R cjsrb = kSS ? s_sc[2][tid] : L.cjsrb[g], ancx = kSS ? s_sc[3][tid] : L.ancx[g];
@@ -727,6 +528,232 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       a.diag[(int64_t)D_XICAT * S + g] = (double)icat1;
     }
     tstat = status;
+
+    // the channel part above reads no halo; the sub-voxel part below needs
+    // this thread's halo copies
+    if (kStage) cp_async_wait_group<0>();
+
+    // ---- sub-voxel diffusion, SERCA/leak, cytosolic buffers (:1305-1393) ----
+    // Processed as four z-pairs p = (sub-voxels 2p, 2p+1).  Along z the pair's
+    // halves are each other's neighbour; the outer neighbours are the
+    // adjacent CRUs' pair p.  Along y (x) the neighbour pair is p^1 (p^2) of
+    // this CRU or of the adjacent CRU in the direction of the pair's y (x)
+    // bit.  At a lattice face the zero-flux ghost equals the sub-voxel
+    // itself (:1601-1652), so that difference vanishes.
+    const bool has_yp = y + 1 < ly, has_ym = y > 0;
+    const bool has_xp = x + 1 < lx, has_xm = x > 0;
+    const bool zp_in = tid + lxly < count, zm_in = tid - lxly >= 0;
+    const bool yp_in = tid + lx < count, ym_in = tid - lx >= 0;
+    const bool xp_in = tid + 1 < count, xm_in = tid - 1 >= 0;
+    const V kt_n = splat2(R(1.0 / (TAUNT * XI))), kl_n = splat2(R(1.0 / (TAUNL * XI)));
+    const V kt_i = splat2(R(1.0 / (TAUIT * XI))), kl_i = splat2(R(1.0 / (TAUIL * XI)));
+    const V dt2 = splat2(dt);
+    const V* catf2 = reinterpret_cast<const V*>(L.catf);
+    const V* cats2 = reinterpret_cast<const V*>(L.cats);
+    const V* cacal2 = reinterpret_cast<const V*>(L.cacal);
+    const V* casr2 = reinterpret_cast<const V*>(L.casr);
+    const V* camyo2 = reinterpret_cast<const V*>(L.camyo);
+    const V* mgmyo2 = reinterpret_cast<const V*>(L.mgmyo);
+    V* catf2w = reinterpret_cast<V*>(L.catf);
+    V* cats2w = reinterpret_cast<V*>(L.cats);
+    V* cacal2w = reinterpret_cast<V*>(L.cacal);
+    V* casr2w = reinterpret_cast<V*>(L.casr);
+    V* camyo2w = reinterpret_cast<V*>(L.camyo);
+    V* mgmyo2w = reinterpret_cast<V*>(L.mgmyo);
+    R sum_ci = R(0), sum_cn = R(0), sum_catf = R(0), sum_cats = R(0), sum_casr = R(0);
+    R sum_camyo = R(0), sum_cacal = R(0), sum_up = R(0), sum_lk = R(0);
+    bool ci_high = false;
+#pragma unroll 1
+    for (int p = 0; p < 4; ++p) {
+      const int by = p & 1, bx = p >> 1;
+      const int64_t gp = p * S + g;
+      const V c = s_ci2[p][tid], n = s_cn2[p][tid];
+      constexpr bool kSB = TS::kStageBuf;
+      V catf = kSB ? s_buf[0][p][tid] : nb0, cats = kSB ? s_buf[1][p][tid] : nb1;
+      V cacal = kSB ? s_buf[2][p][tid] : nb2, casr = kSB ? s_buf[3][p][tid] : nb3;
+      V camyo = kSB ? s_buf[4][p][tid] : nb4, mgmyo = kSB ? s_buf[5][p][tid] : nb5;
+      if (!kSB && p < 3) {
+        const int64_t gq = gp + S;
+        nb0 = catf2[gq], nb1 = cats2[gq], nb2 = cacal2[gq], nb3 = casr2[gq], nb4 = camyo2[gq];
+        nb5 = mgmyo2[gq];
+      }
+      // z
+      V czp = c, nzp = n, czm = c, nzm = n;
+      if (kStage) {
+        if (has_zp) {
+          czp.x = s_hz[1][p][0][tid];
+          nzp.x = s_hz[1][p][1][tid];
+        }
+        if (has_zm) {
+          czm.y = s_hz[0][p][0][tid];
+          nzm.y = s_hz[0][p][1][tid];
+        }
+      } else {
+      if (has_zp) {
+        if (zp_in) {
+          czp = s_ci2[p][tid + lxly];
+          nzp = s_cn2[p][tid + lxly];
+        } else {
+          czp = __ldg(ci2 + gp + lxly);
+          nzp = __ldg(cn2 + gp + lxly);
+        }
+      }
+      if (has_zm) {
+        if (zm_in) {
+          czm = s_ci2[p][tid - lxly];
+          nzm = s_cn2[p][tid - lxly];
+        } else {
+          czm = __ldg(ci2 + gp - lxly);
+          nzm = __ldg(cn2 + gp - lxly);
+        }
+      }
+      }
+      const V ciN = v2(c.y, has_zp ? czp.x : c.y), cnN = v2(n.y, has_zp ? nzp.x : n.y);
+      const V ciS = v2(has_zm ? czm.y : c.x, c.x), cnS = v2(has_zm ? nzm.y : n.x, n.x);
+      // y: pair p^1
+      V ciE, cnE, ciW, cnW;
+      {
+        const int py = p ^ 1;
+        const V ci_in = s_ci2[py][tid], cn_in = s_cn2[py][tid];
+        V ci_ex = c, cn_ex = n;
+        const int d = by ? lx : -lx;
+        if (by ? has_yp : has_ym) {
+          if (kStage) {
+            ci_ex = s_hy[by][p >> 1][0][tid];
+            cn_ex = s_hy[by][p >> 1][1][tid];
+          } else if (by ? yp_in : ym_in) {
+            ci_ex = s_ci2[py][tid + d];
+            cn_ex = s_cn2[py][tid + d];
+          } else {
+            ci_ex = __ldg(ci2 + py * S + g + d);
+            cn_ex = __ldg(cn2 + py * S + g + d);
+          }
+        }
+        ciE = by ? ci_ex : ci_in;
+        cnE = by ? cn_ex : cn_in;
+        ciW = by ? ci_in : ci_ex;
+        cnW = by ? cn_in : cn_ex;
+      }
+      // x: pair p^2
+      V ciT, cnT, ciB, cnB;
+      {
+        const int px = p ^ 2;
+        const V ci_in = s_ci2[px][tid], cn_in = s_cn2[px][tid];
+        V ci_ex = c, cn_ex = n;
+        const int d = bx ? 1 : -1;
+        if (bx ? has_xp : has_xm) {
+          if (bx ? xp_in : xm_in) {
+            ci_ex = s_ci2[px][tid + d];
+            cn_ex = s_cn2[px][tid + d];
+          } else if (kStage) {
+            ci_ex = s_hx[bx][px][0];
+            cn_ex = s_hx[bx][px][1];
+          } else {
+            ci_ex = __ldg(ci2 + px * S + g + d);
+            cn_ex = __ldg(cn2 + px * S + g + d);
+          }
+        }
+        ciT = bx ? ci_ex : ci_in;
+        cnT = bx ? cn_ex : cn_in;
+        ciB = bx ? ci_in : ci_ex;
+        cnB = bx ? cn_in : cn_ex;
+      }
+      const V coupn = vfma(vadd(vadd(vadd(vsub(cnN, n), vsub(cnS, n)), vsub(cnE, n)), vsub(cnW, n)),
+                           kt_n, vmul(vadd(vsub(cnT, n), vsub(cnB, n)), kl_n));
+      const V coupi = vfma(vadd(vadd(vadd(vsub(ciN, c), vsub(ciS, c)), vsub(ciE, c)), vsub(ciW, c)),
+                           kt_i, vmul(vadd(vsub(ciT, c), vsub(ciB, c)), kl_i));
+      // SERCA and leak (subroutine_cuda.c:128-146)
+      V up, lk;
+      {
+        const R pax = Math<R>::powpos(c.x * R(1.0 / KI_UP), R(HH_UP));
+        const R pay = Math<R>::powpos(c.y * R(1.0 / KI_UP), R(HH_UP));
+        const R pbx = Math<R>::powpos(n.x * R(1.0 / KNSR_UP), R(HH_UP));
+        const R pby = Math<R>::powpos(n.y * R(1.0 / KNSR_UP), R(HH_UP));
+        up = v2(k.sviup * Math<R>::div(R(VUP) * (pax - pbx), R(1) + pax + pbx),
+                k.sviup * Math<R>::div(R(VUP) * (pay - pby), R(1) + pay + pby));
+        const V n2 = vmul(n, n);
+        const V num = vmul(vmul(splat2(R(GLEAK)), vsub(n, c)), n2);
+        const V den = vadd(n2, splat2(R(KJSR_LEAK * KJSR_LEAK)));
+        lk = v2(Math<R>::div(num.x, den.x), Math<R>::div(num.y, den.y));
+      }
+      // cytosolic buffers (buffers.c:55-115): on*(B-b) - koff*b, with the
+      // saturation guard kon*c*dt > 1 taken on the rare slow path
+      const V freemyo = vsub(vsub(splat2(R(BMYO)), camyo), mgmyo);
+      V r_tf = vfma(vmul(splat2(R(KTFON)), c), vsub(splat2(R(BTF)), catf), vmul(splat2(R(-KTFOFF)), catf));
+      V r_ts = vfma(vmul(splat2(R(KTSON)), c), vsub(splat2(R(BTS)), cats), vmul(splat2(R(-KTSOFF)), cats));
+      V r_cal = vfma(vmul(splat2(R(KCALON)), c), vsub(splat2(R(BCAL)), cacal),
+                     vmul(splat2(R(-KCALOFF)), cacal));
+      V r_sr = vfma(vmul(splat2(R(KSRON)), c), vsub(splat2(R(BSR)), casr), vmul(splat2(R(-KSROFF)), casr));
+      V r_mc = vfma(vmul(splat2(R(KONMYOCA)), c), freemyo, vmul(splat2(R(-KOFFMYOCA)), camyo));
+      if (fmax(c.x, c.y) * R(KONMYOCA) * dt > R(1)) {  // some buffer saturates
+        const R cc[2] = {c.x, c.y};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const R cv = cc[h];
+          R& tf = h ? r_tf.y : r_tf.x;
+          R& ts = h ? r_ts.y : r_ts.x;
+          R& cal = h ? r_cal.y : r_cal.x;
+          R& sr = h ? r_sr.y : r_sr.x;
+          R& mc = h ? r_mc.y : r_mc.x;
+          tf = buffer_rate<R>(R(KTFON), R(KTFOFF), R(BTF), h ? catf.y : catf.x, cv, dt, k.rdt95);
+          ts = buffer_rate<R>(R(KTSON), R(KTSOFF), R(BTS), h ? cats.y : cats.x, cv, dt, k.rdt95);
+          cal = buffer_rate<R>(R(KCALON), R(KCALOFF), R(BCAL), h ? cacal.y : cacal.x, cv, dt, k.rdt95);
+          sr = buffer_rate<R>(R(KSRON), R(KSROFF), R(BSR), h ? casr.y : casr.x, cv, dt, k.rdt95);
+          const R fmy = h ? freemyo.y : freemyo.x;
+          const R cm = h ? camyo.y : camyo.x;
+          const R onmc = R(KONMYOCA) * cv;
+          mc = (onmc * dt > R(1)) ? k.rdt95 * fmy - R(KOFFMYOCA) * cm : onmc * fmy - R(KOFFMYOCA) * cm;
+        }
+      }
+      V dotcn = vfma(vsub(up, lk), splat2(R(VI / VNSR)), coupn);
+      V dotci = vadd(vsub(vsub(lk, up), vadd(vadd(vadd(vadd(r_tf, r_ts), r_cal), r_sr), r_mc)), coupi);
+      if (p == 0) {  // sub-voxels 0 and 1 touch the dyad, submembrane and JSR (:1356-1361)
+        dotcn = vfma(v2(diffjn0, diffjn1), splat2(R(VJSR / VNSR)), dotcn);
+        dotci = vfma(v2(diffsi0, diffsi1), splat2(R(VS / VI)), dotci);
+        dotci = vfma(v2(diffpi0, diffpi1), splat2(R(VP / VI)), dotci);
+      }
+      const V cinew = vclamp0(vfma(dotci, dt2, c));
+      const V cnnew = vfma(dotcn, dt2, n);
+      catf = vclamp0(vfma(r_tf, dt2, catf));
+      cats = vclamp0(vfma(r_ts, dt2, cats));
+      cacal = vclamp0(vfma(r_cal, dt2, cacal));
+      casr = vclamp0(vfma(r_sr, dt2, casr));
+      camyo = vclamp0(vfma(r_mc, dt2, camyo));
+      {
+        const V fm = vsub(vsub(splat2(R(BMYO)), camyo), mgmyo);
+        V r_mg = vfma(splat2(R(KONMYOMG * MGI)), fm, vmul(splat2(R(-KOFFMYOMG)), mgmyo));
+        if (R(KONMYOMG * MGI) * dt > R(1)) {  // guard of myomg (buffers.c:65)
+          r_mg = vfma(splat2(k.rdt95), fm, vmul(splat2(R(-KOFFMYOMG)), mgmyo));
+        }
+        mgmyo = vclamp0(vfma(r_mg, dt2, mgmyo));
+      }
+      cinext2[gp] = cinew;
+      cnnext2[gp] = cnnew;
+      catf2w[gp] = catf;
+      cats2w[gp] = cats;
+      cacal2w[gp] = cacal;
+      casr2w[gp] = casr;
+      camyo2w[gp] = camyo;
+      mgmyo2w[gp] = mgmyo;
+      if (a.diag) {
+        a.diag[(int64_t)(D_XIUP + 2 * p) * S + g] = (double)up.x;
+        a.diag[(int64_t)(D_XIUP + 2 * p + 1) * S + g] = (double)up.y;
+        a.diag[(int64_t)(D_XILEAK + 2 * p) * S + g] = (double)lk.x;
+        a.diag[(int64_t)(D_XILEAK + 2 * p + 1) * S + g] = (double)lk.y;
+      }
+      if (OUT && out_step) {
+        sum_ci += cinew.x + cinew.y;
+        sum_cn += cnnew.x + cnnew.y;
+        sum_catf += catf.x + catf.y;
+        sum_cats += cats.x + cats.y;
+        sum_casr += casr.x + casr.y;
+        sum_camyo += camyo.x + camyo.y;
+        sum_cacal += cacal.x + cacal.y;
+        sum_up += up.x + up.y;
+        sum_lk += lk.x + lk.y;
+        ci_high |= (cinew.x > R(1000)) || (cinew.y > R(1000));
+      }
+    }
 
     p_cs = csn;
     p_xicat = icat1;
