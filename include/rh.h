@@ -60,8 +60,8 @@ extern "C" {
                                          Gaussian draw is then NaN, is redrawn up to
                                          the 200-try cap and counts 0 */
 
-#define RH_STATUS_TIMEOUT 0x20u       /* a bounded wait for a tile's bulk copies ran
-                                         out; that tile was not updated */
+#define RH_STATUS_TIMEOUT 0x20u       /* reserved for a bounded device wait that ran
+                                         out (the kernels of this build have none) */
 
 /* Number of columns of one wholecell record and one linescan row. */
 #define RH_WHOLECELL_COLS 45
