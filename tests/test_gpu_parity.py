@@ -240,3 +240,29 @@ def test_tile_sizes_agree_and_autotune_leaves_state_unchanged():
         for c in range(2):
             for k in ("nou", "ncb", "lcc"):
                 np.testing.assert_array_equal(a.get_state(c)[k], b.get_state(c)[k])
+
+
+def test_cell_groups_give_identical_results():
+    """Cells advance independently and the whole-cell sums are exact, so how
+    the cells are grouped onto concurrent streams changes no bit of the
+    state, the membrane or the output records."""
+    cells = [c1_params(nx=14 + 3 * i, ny=8 + i, nz=5, seed=3, cell_id=i, ku2=1.0 + 0.4 * i)
+             for i in range(5)]
+    for precision in ("mixed", "fp64"):
+        runs = []
+        for groups in (1, 2, 5):
+            with Simulator(cells, precision=precision, cell_groups=groups) as sim:
+                assert (sim.num_groups() == 1) == (groups == 1)  # about equal CRU counts
+                sim.run_steps(450)  # four output windows and a partial one
+                runs.append(([sim.get_state(c).snapshot() for c in range(5)],
+                             [sim.get_membrane(c) for c in range(5)],
+                             [sim.drain_wholecell(c) for c in range(5)],
+                             [sim.status(c) for c in range(5)]))
+        st0, m0, wc0, s0 = runs[0]
+        for st, m, wc, s in runs[1:]:
+            assert s == s0
+            for c in range(5):
+                for k in st0[c]:
+                    np.testing.assert_array_equal(st[c][k], st0[c][k], err_msg=f"{precision} {k}")
+                assert m[c].v == m0[c].v and m[c].xnai == m0[c].xnai and m[c].t == m0[c].t
+                np.testing.assert_array_equal(wc[c], wc0[c])
