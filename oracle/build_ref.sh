@@ -57,6 +57,8 @@ declare -A VARIANTS=(
   [small_il]="-Dnx=12 -Dny=9 -Dnz=7 -Dnbeat=1 -Dtperid=1000.0 -DREF_LINESCAN_JZ=5 -Diso2 -Dlqt"
   # the shipped 64x28x12 make-il build
   [default_il]="-Diso2 -Dlqt -DREF_LINESCAN_JZ=5"
+  # small_il with the reference's cadist_ writer enabled (#define outputcadist)
+  [small_il_cd]="-Dnx=12 -Dny=9 -Dnz=7 -Dnbeat=1 -Dtperid=1000.0 -DREF_LINESCAN_JZ=5 -Diso2 -Dlqt -Doutputcadist"
 )
 want=("$@")
 if [ ${#want[@]} -eq 0 ]; then want=("${!VARIANTS[@]}"); fi

@@ -61,6 +61,8 @@ def lib() -> C.CDLL:
         L.orc_last_wholecell.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_last_linescan.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_last_linescan.restype = C.c_int32
+        L.orc_last_cadist.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.orc_last_cadist.restype = C.c_int32
         L.orc_protocol_done.argtypes = [C.c_void_p]
         L.orc_protocol_done.restype = C.c_int32
         L.orc_status.argtypes = [C.c_void_p]
@@ -141,6 +143,19 @@ class Oracle:
                                      C.byref(nrec))
         return t[:done].copy(), v[:done].copy(), wc[: nrec.value].copy()
 
+    def run_cadist(self, nsteps: int) -> list[np.ndarray]:
+        """Runs nsteps and returns the cadist records written on the way
+        (each: t, v, then 6 values per interior CRU, reference order)."""
+        recs = []
+        buf = np.zeros(2 + 6 * self.n)
+        for _ in range(int(nsteps)):
+            if self.done:
+                break
+            self.L.orc_step(self.h)
+            if self.L.orc_last_cadist(self.h, _dptr(buf)):
+                recs.append(buf.copy())
+        return recs
+
     def get_state(self) -> HostState:
         hs = HostState(self.n)
         self.L.orc_get_state(self.h, C.byref(hs.view))
@@ -180,6 +195,16 @@ def wholecell_text(rows) -> str:
     return "".join(format_wholecell(r) for r in rows)
 
 
+def cadist_text(records) -> str:
+    """The reference's cadist_ file for these records (:1005, :1009)."""
+    out = []
+    for r in records:
+        out.append("0 header %f %f\n" % (r[0], r[1]))
+        rows = np.asarray(r[2:]).reshape(-1, 6)
+        out.extend("%f %f %f %f %f %f\n" % tuple(x) for x in rows)
+    return "".join(out)
+
+
 def linescan_text(blocks) -> str:
     out = []
     for b in blocks:
@@ -215,3 +240,9 @@ def run_ref(variant: str, args, workdir: str, max_steps: int | None = None,
     with open(os.path.join(workdir, f"linescan_{name}")) as f:
         ls = f.read()
     return wt, ls
+
+
+def ref_cadist(workdir: str) -> str:
+    """Text of the cadist_ file of the last run_ref in workdir."""
+    with open(os.path.join(workdir, "cadist_ref")) as f:
+        return f.read()

@@ -151,6 +151,8 @@ struct orc_sim {
   rh_membrane m;
   double wc[RH_WHOLECELL_COLS];
   double* ls; /* (nx-2) x 22 */
+  double* cd; /* cadist record: t, v, then 6 values per interior CRU */
+  int cd_valid;
 };
 
 static inline int opos(const orc_sim* s, int i, int j, int k) {
@@ -898,6 +900,31 @@ static void membrane_update(orc_sim* s) {
 }
 
 /* Output statistics at an output step (cuda_Cell_Detailed.cu:788-1079). */
+/* cadist record (cuda_Cell_Detailed.cu:1001-1013, the outputcadist build):
+ * every 5 ms during the first 500 ms of each pacing period, "0 header t v"
+ * and per interior CRU (jx outer, jz inner) ci of sub-voxel 0, cs, cp, cjsr,
+ * xinaca/Cm*0.0965*Vs*16120 and xire. */
+static void cadist_record(orc_sim* s) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  const double* ci = s->ci[s->cur];
+  const double* cs = s->cs[s->cur];
+  double* r = s->cd;
+  *r++ = s->m.t;
+  *r++ = s->m.v;
+  for (int jx = 1; jx < nx - 1; jx++)
+    for (int jy = 1; jy < ny - 1; jy++)
+      for (int jz = 1; jz < nz - 1; jz++) {
+        const int ac = opos(s, jx, jy, jz);
+        *r++ = ci[ac * 8];
+        *r++ = cs[ac];
+        *r++ = s->cp[ac];
+        *r++ = s->cjsr[ac];
+        *r++ = s->xinaca[ac] / CM * 0.0965 * VS * 16120.;
+        *r++ = s->xire[ac];
+      }
+  s->cd_valid = 1;
+}
+
 static void output_record(orc_sim* s) {
   const int nx = s->nx, ny = s->ny, nz = s->nz;
   const double* ci = s->ci[s->cur];
@@ -1092,9 +1119,12 @@ int orc_step(orc_sim* s) {
   wholecell_reduce(s);
   membrane_update(s);
   int out = 0;
+  s->cd_valid = 0;
   if (fmod(s->m.t + 0.0000001, OUTT) < s->dt) { /* :777 */
     output_record(s);
     out = 1;
+    if (fmod(s->m.t + 0.0000001, 5) < s->dt && fmod(s->m.t + 0.0000001, s->p.pcl_ms) < 500)
+      cadist_record(s); /* :1002 */
   }
   s->m.t = s->m.t + s->dt; /* :1083 */
   return out;
@@ -1184,8 +1214,9 @@ orc_sim* orc_create(const rh_cell_params* p, double dt) {
   ALLOC(s->ci[0], n8); ALLOC(s->ci[1], n8); ALLOC(s->cnsr[0], n8); ALLOC(s->cnsr[1], n8);
   ALLOC(s->cs[0], n1); ALLOC(s->cs[1], n1);
   ALLOC(s->ls, (size_t)(p->nx - 2) * RH_LINESCAN_COLS);
+  ALLOC(s->cd, 2 + (size_t)s->nin * 6);
 #undef ALLOC
-  if (!s->ls || !s->cs[1]) {
+  if (!s->ls || !s->cs[1] || !s->cd) {
     orc_destroy(s);
     return NULL;
   }
@@ -1215,7 +1246,7 @@ void orc_destroy(orc_sim* s) {
   double* dp[] = {s->cp, s->cjsr, s->cjsrb, s->ancx, s->xire, s->po, s->xinaca, s->xicat,
                   s->casar, s->casarh, s->casarj, s->casarhj, s->xiup, s->xileak, s->catf,
                   s->cats, s->cacal, s->casr, s->camyo, s->mgmyo, s->cadye, s->ci[0], s->ci[1],
-                  s->cnsr[0], s->cnsr[1], s->cs[0], s->cs[1], s->ls};
+                  s->cnsr[0], s->cnsr[1], s->cs[0], s->cs[1], s->ls, s->cd};
   for (size_t q = 0; q < sizeof(dp) / sizeof(dp[0]); ++q) free(dp[q]);
   int* ip[] = {s->lcc, s->nl, s->nou, s->ncu, s->nob, s->ncb, s->nspark};
   for (size_t q = 0; q < sizeof(ip) / sizeof(ip[0]); ++q) free(ip[q]);
@@ -1294,6 +1325,12 @@ void orc_last_wholecell(const orc_sim* s, double* cols45) {
 int32_t orc_last_linescan(const orc_sim* s, double* rows) {
   if (rows) memcpy(rows, s->ls, sizeof(double) * (s->nx - 2) * RH_LINESCAN_COLS);
   return s->nx - 2;
+}
+
+int32_t orc_last_cadist(const orc_sim* s, double* rec) {
+  if (!s->cd_valid) return 0;
+  if (rec) memcpy(rec, s->cd, sizeof(double) * (2 + (size_t)s->nin * 6));
+  return s->nin;
 }
 
 uint32_t orc_status(const orc_sim* s) { return s->status; }

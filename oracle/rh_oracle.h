@@ -61,6 +61,10 @@ void orc_set_membrane(orc_sim* s, const rh_membrane* src);
 /* Last output record / linescan block (valid after orc_step returned 1). */
 void orc_last_wholecell(const orc_sim* s, double* cols45);
 int32_t orc_last_linescan(const orc_sim* s, double* rows);
+/* cadist record of the last step (t, v, then 6 values per interior CRU in the
+ * reference's jx-outer order) if that step wrote one: returns the number of
+ * CRUs, else 0. */
+int32_t orc_last_cadist(const orc_sim* s, double* rec);
 
 int32_t orc_protocol_done(const orc_sim* s);
 uint32_t orc_status(const orc_sim* s);

@@ -9,6 +9,10 @@ Fixtures (all produced by running the reference's own code):
   ref_<variant>_linescan_head.txt    first linescan_ blocks of the run
   ref_full_runs.json                 sha256 and line counts of the complete
                                      wholetest_/linescan_ files of each run
+  ref_small_il_cd_cadist_head.txt    first record of the cadist_ file of the
+                                     small_il build with outputcadist defined,
+                                     run for CADIST_STEPS steps (its sha256 is in
+                                     ref_full_runs.json under "small_il_cd")
 """
 from __future__ import annotations
 
@@ -36,6 +40,8 @@ RUNS = {
                      cell=dict(nx=12, ny=9, nz=7, nbeats=1, pcl_ms=1000.0, lqt=1, iso2=1,
                                linescan_jz=-1)),
 }
+CADIST_VARIANT = "small_il_cd"  # small_il with the cadist_ writer enabled
+CADIST_STEPS = 1700
 HEAD_WHOLETEST_LINES = 40
 HEAD_LINESCAN_BLOCKS = 6
 
@@ -59,6 +65,16 @@ def main() -> None:
                              wholetest_sha256=sha(wt), wholetest_lines=len(wt_lines),
                              linescan_sha256=sha(ls), linescan_lines=len(ls.splitlines()))
         print(variant, meta[variant]["wholetest_lines"], "wholetest lines")
+    spec = RUNS["small_il"]
+    with tempfile.TemporaryDirectory() as d:
+        O.run_ref(CADIST_VARIANT, spec["args"], d, max_steps=CADIST_STEPS)
+        cd = O.ref_cadist(d)
+    first = cd.split("0 header")[1]
+    with open(os.path.join(HERE, f"ref_{CADIST_VARIANT}_cadist_head.txt"), "w") as f:
+        f.write("0 header" + first)
+    meta[CADIST_VARIANT] = dict(args=spec["args"], cell=spec["cell"], seed=18, steps=CADIST_STEPS,
+                                cadist_sha256=sha(cd), cadist_records=cd.count("0 header"))
+    print(CADIST_VARIANT, meta[CADIST_VARIANT]["cadist_records"], "cadist records")
     with open(os.path.join(HERE, "ref_full_runs.json"), "w") as f:
         json.dump(meta, f, indent=1)
 

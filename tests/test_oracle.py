@@ -40,6 +40,20 @@ def test_oracle_matches_reference_head(variant):
     assert O.linescan_text(ls[:nblk]) == want_ls
 
 
+def test_oracle_cadist_matches_reference():
+    """The cadist_ writer (cuda_Cell_Detailed.cu:1001-1013, built with
+    outputcadist): first record byte for byte, all records by sha256."""
+    p, _ = _params("small_il")
+    spec = META["small_il_cd"]
+    o = O.Oracle(p)
+    recs = o.run_cadist(spec["steps"])
+    text = O.cadist_text(recs)
+    assert len(recs) == spec["cadist_records"]
+    want = open(os.path.join(GOLD, "ref_small_il_cd_cadist_head.txt")).read()
+    assert O.cadist_text(recs[:1]) == want
+    assert hashlib.sha256(text.encode()).hexdigest() == spec["cadist_sha256"]
+
+
 @pytest.mark.slow
 def test_oracle_matches_reference_full_run():
     p, spec = _params("c1")
