@@ -66,6 +66,7 @@ extern "C" {
 /* Number of columns of one wholecell record and one linescan row. */
 #define RH_WHOLECELL_COLS 45
 #define RH_LINESCAN_COLS 22
+#define RH_CADIST_COLS 6 /* per interior CRU; a record adds t and V */
 
 /* Parameters of one cell.  argv[k] refers to the reference command line
  * (cuda_Cell_Detailed <dev> <name> a3 .. a10). */
@@ -110,6 +111,12 @@ typedef struct {
   int32_t cell_groups;        /* cells split into this many groups of about equal
                                  CRU count that advance on concurrent streams
                                  (0 = 4; capped at the number of cells) */
+  int32_t record_cadist;      /* 1 = keep cadist records (the reference's
+                                 outputcadist build, :1001-1013): every 5 ms in the
+                                 first 500 ms of each pacing period, t, V and 6
+                                 values per interior CRU */
+  int32_t cadist_capacity;    /* cadist records kept per cell between drains
+                                 (0 = 8) */
 } rh_run_opts;
 
 /* Full FP64 view of one cell's lattice state (caller-owned host arrays of
@@ -198,6 +205,13 @@ int rh_drain_linescan(rh_sim* sim, int32_t cell, double* rows, int32_t max_rec,
                       int32_t* nrec);
 int rh_drain_stats(rh_sim* sim, int32_t cell, rh_beat_stats* out, int32_t max_rec,
                    int32_t* nrec);
+
+/* cadist records produced since the last drain (run option record_cadist):
+ * each is 2 + 6*n doubles (n interior CRUs), t and V, then per CRU in the
+ * reference's order (jx outer, jy, jz inner) ci of sub-voxel 0, cs, cp, cjsr,
+ * xinaca/Cm*0.0965*Vs*16120 and xire, the values the reference prints
+ * (:1005, :1009).  Returns RH_ERR_ARG when record_cadist is off. */
+int rh_drain_cadist(rh_sim* sim, int32_t cell, double* rec, int32_t max_rec, int32_t* nrec);
 
 /* Per-beat statistics of a recorded trace, with the same detectors the
  * simulator runs on the GPU (for traces produced elsewhere, e.g. by a CPU

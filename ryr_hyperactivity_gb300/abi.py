@@ -60,6 +60,8 @@ class RunOpts(C.Structure):
         ("keep_diagnostics", C.c_int32),
         ("window_steps", C.c_int32),
         ("cell_groups", C.c_int32),
+        ("record_cadist", C.c_int32),
+        ("cadist_capacity", C.c_int32),
     ]
 
 

@@ -180,6 +180,8 @@ __host__ __device__ inline bool step_coef(StepCoef<double>& k, const rh_membrane
   k.rdth95 = 0.95 / (dt / 5.0);
   k.reset_window = fmod(t - dt, OUTT) < dt;
   k.output_step = fmod(t + 0.0000001, OUTT) < dt;
+  k.cadist_step = k.output_step && fmod(t + 0.0000001, 5.0) < dt &&
+                  fmod(t + 0.0000001, c.pcl) < 500.0;  // :1002
   return t < c.tend;
 }
 

@@ -140,10 +140,11 @@ struct WarpSlots {
 // doubles of shared memory owned by the warp.  The lattice sums come in as
 // tot (sum cs, sum xicat, sum xinaca over the cell's CRUs, :447-456); the
 // function also computes the three fmods of this step (stimulus phase and the
-// next lattice update's window flags) into fm[0..2].
+// next lattice update's window flags: reset, output, and the two cadist
+// conditions) into fm[0..4].
 __device__ inline void membrane_update_warp(rh_membrane& m, double dt, double tperid,
                                             double svikr, const double tot[3], int nin,
-                                            double* s, double fm[3]) {
+                                            double* s, double fm[5]) {
   const int lane = threadIdx.x & 31;
   WarpSlots w{s, s + 32, s + 64, lane};
   const double t = m.t, v = m.v;
@@ -180,15 +181,15 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, double tp
   const double pw = pow(lane == 0 ? q28 : q12, lane == 0 ? 3.0 : 1.00);
   const double pow_ks = __shfl_sync(0xffffffffu, pw, 0);
   const double pow_nak = __shfl_sync(0xffffffffu, pw, 1);
-  // fmods: stimulus phase (:689) and the next update's window flags (:1244, :777)
+  // fmods: stimulus phase (:689) and the next update's window, output and
+  // cadist flags (:1244, :777, :1002)
   {
     const double tn = t + dt;
     const double x = lane == 0 ? t + tperid - 100 : (lane == 1 ? tn - dt : tn + 0.0000001);
-    const double y = lane == 0 ? tperid : OUTT;
+    const double y = lane == 0 ? tperid : lane == 3 ? 5.0 : lane == 4 ? tperid : OUTT;
     const double f = fmod(x, y);
-    fm[0] = __shfl_sync(0xffffffffu, f, 0);
-    fm[1] = __shfl_sync(0xffffffffu, f, 1);
-    fm[2] = __shfl_sync(0xffffffffu, f, 2);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) fm[i] = __shfl_sync(0xffffffffu, f, i);
   }
 
   // ---- round 1: the voltage exponentials, one per lane ----
@@ -352,12 +353,14 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, double tp
 }
 
 // Coefficients of the next lattice update (step_coef, cellmodel.cuh) by one
-// warp; fm1, fm2 are fmod(t - dt, OUTT) and fmod(t + 1e-7, OUTT) for the
-// state's time t; `s` is 96 doubles of shared memory owned by the warp.
-// Returns whether the cell is inside its protocol.
+// warp; fm holds fmod(t - dt, OUTT), fmod(t + 1e-7, OUTT), fmod(t + 1e-7, 5)
+// and fmod(t + 1e-7, PCL) for the state's time t (entries 1..4 of
+// membrane_update_warp's fm); `s` is 96 doubles of shared memory owned by the
+// warp.  Returns whether the cell is inside its protocol.
 __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
-                                      const CellConst& c, double dt, double fm1, double fm2,
+                                      const CellConst& c, double dt, const double* fm,
                                       double* s) {
+  const double fm1 = fm[0], fm2 = fm[1];
   const int lane = threadIdx.x & 31;
   WarpSlots w{s, s + 32, s + 64, lane};
   const double v = m.v, xnai = m.xnai, t = m.t;
@@ -454,6 +457,7 @@ __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
   k.dt = dt;
   k.reset_window = fm1 < dt;
   k.output_step = fm2 < dt;
+  k.cadist_step = k.output_step && fm[2] < dt && fm[3] < 500;
   return t < c.tend;
 }
 

@@ -6,13 +6,15 @@
 // Positional arguments keep the reference's meaning (run.sh:7-9):
 //   a3 clamp voltage, a4 cjsr_basal, a5 NCX scale, a6 Ku, a7 r1 (unused),
 //   a8 Kb, a9 ICaL scale, a10 Ku2.
-// Writes wholetest_<name>, linescan_<name> and (empty, as the reference does
-// by default) cadist_<name> in the same formats, prints "Initialization
-// Complete" and exits 0.  The reference's compile-time switches become
+// Writes wholetest_<name>, linescan_<name> and cadist_<name> in the same
+// formats (cadist_ stays empty, as in the reference's default build, unless
+// --cadist selects the outputcadist build), prints "Initialization Complete"
+// and exits 0.  The reference's compile-time switches become
 // options; the defaults are the run.sh build (make il) on the shipped
 // 64x28x12 lattice, PCL 4000 ms, 7 beats:
 //   --nx N --ny N --nz N --nbeats N --pcl MS   lattice and protocol
 //   --lqt 0|1 --iso2 0|1 --tapsi 0|1           build modes (Makefile:8-28)
+//   --cadist                                   outputcadist build (:1001-1013)
 //   --mixed                                    FP32 lattice / FP64 whole-cell
 //   --seed S --ikr-scale X --cao MM --linescan-jz J --max-steps N
 #include <stdio.h>
@@ -28,7 +30,7 @@
 static void usage() {
   fprintf(stderr,
           "usage: cuda_Cell_Detailed <device> <name> a3 a4 a5 a6 a7 a8 a9 a10 [--nx N] [--ny N] "
-          "[--nz N] [--nbeats N] [--pcl MS] [--lqt 0|1] [--iso2 0|1] [--tapsi 0|1] [--mixed] "
+          "[--nz N] [--nbeats N] [--pcl MS] [--lqt 0|1] [--iso2 0|1] [--tapsi 0|1] [--cadist] [--mixed] "
           "[--seed S] [--ikr-scale X] [--cao MM] [--linescan-jz J] [--max-steps N]\n");
 }
 
@@ -71,6 +73,7 @@ int main(int argc, char** argv) {
     else if (k == "--iso2") p.iso2 = atoi(next());
     else if (k == "--tapsi") p.tapsi = atoi(next());
     else if (k == "--mixed") o.precision = RH_MIXED;
+    else if (k == "--cadist") o.record_cadist = 1;
     else if (k == "--seed") p.seed = (uint32_t)strtoul(next(), nullptr, 10);
     else if (k == "--ikr-scale") p.ikr_scale = atof(next());
     else if (k == "--cao") p.cao_mM = atof(next());
@@ -90,6 +93,7 @@ int main(int argc, char** argv) {
   }
   o.window_steps = 100;
   o.output_capacity = 64;
+  o.cadist_capacity = 8;  // one record per 200 steps at most; drained every 100
   rh_sim* sim = nullptr;
   int rc = rh_create(&p, 1, &o, &sim);
   if (rc != RH_OK) {
@@ -102,6 +106,9 @@ int main(int argc, char** argv) {
   fflush(stdout);
   const int lx = p.nx - 2;
   std::vector<double> wc(64 * RH_WHOLECELL_COLS), ls((size_t)64 * lx * RH_LINESCAN_COLS);
+  const size_t ncru = (size_t)(p.nx - 2) * (p.ny - 2) * (p.nz - 2);
+  const size_t cd_len = 2 + RH_CADIST_COLS * ncru;
+  std::vector<double> cd(o.record_cadist ? 8 * cd_len : 0);
   char line[4096];
   long long steps = 0;
   uint32_t reported = 0;
@@ -117,6 +124,20 @@ int main(int argc, char** argv) {
     if (rc != RH_OK) break;
     rc = rh_drain_linescan(sim, 0, ls.data(), 64, &nls);
     if (rc != RH_OK) break;
+    if (o.record_cadist) {  // :1005, :1009
+      int32_t ncd = 0;
+      rc = rh_drain_cadist(sim, 0, cd.data(), 8, &ncd);
+      if (rc != RH_OK) break;
+      for (int r = 0; r < ncd; ++r) {
+        const double* rec = &cd[(size_t)r * cd_len];
+        fprintf(fc, "0 header %f %f\n", rec[0], rec[1]);
+        for (size_t k = 0; k < ncru; ++k) {
+          const double* v = rec + 2 + RH_CADIST_COLS * k;
+          fprintf(fc, "%f %f %f %f %f %f\n", v[0], v[1], v[2], v[3], v[4], v[5]);
+        }
+      }
+      fflush(fc);
+    }
     for (int r = 0; r < nrec; ++r) {
       if (r < nls) {
         for (int x = 0; x < lx; ++x) {

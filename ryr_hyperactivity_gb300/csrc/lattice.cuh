@@ -68,6 +68,7 @@ struct CellConst {
   int iso2;
   uint32_t seed, cell_id;
   long long ls_off;  // first linescan row of this cell in the ring
+  long long cd_off;  // first double of this cell's cadist records (record_cadist)
   double svica, svncx, sviup_tot, svikr, cao, ku, ku2, kb, pcl, tend;
 };
 
@@ -79,10 +80,11 @@ struct CellDyn {
   uint32_t status;
   int parity;
   int done;
-  unsigned int arrive;  // CTAs of this cell that finished the current step
+  unsigned int arrive;  // warps of this cell that finished the current step
   long long out_count;  // output records produced
   BeatTracker bt;       // per-beat statistics in progress
   long long stats_count;  // beat records produced
+  long long cd_count;     // cadist records produced
   // sum cs, xicat, xinaca of the step in progress as 128-bit fixed point
   // (value * 2^64, lo word first), added to by every CTA of the cell and
   // read and cleared by the last one (fixedsum.cuh)
@@ -129,6 +131,8 @@ struct StepArgs {
   double* partials;   // [tile][P_COUNT], by tile-table index
   double* out_wc;     // [cell][cap][45]
   double* out_ls;     // [ls_off + slot*lx + x][22]
+  double* out_cd;     // cadist records, optional: [cd_off + slot*(2 + 6n)]: t, v, 6 per CRU
+  int cd_cap;         // cadist records kept per cell
   double* diag;       // optional
   rh_beat_stats* stats;  // [cell][stats_cap], optional
   int stats_cap;

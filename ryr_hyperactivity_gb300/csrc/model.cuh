@@ -234,6 +234,7 @@ struct StepCoef {
   R dt, rdt, dth, rdt95, rdth95;
   int reset_window;  // fmod(t-dt, outt) < dt (cuda_Cell_Detailed.cu:1244)
   int output_step;   // fmod(t+1e-7, outt) < dt (:777)
+  int cadist_step;   // output step that also writes a cadist record (:1002)
 };
 
 template <class R, class Q>
@@ -246,6 +247,7 @@ __host__ __device__ inline void convert_coef(StepCoef<R>& d, const StepCoef<Q>& 
   d.dt = R(s.dt); d.rdt = R(s.rdt); d.dth = R(s.dth); d.rdt95 = R(s.rdt95); d.rdth95 = R(s.rdth95);
   d.reset_window = s.reset_window;
   d.output_step = s.output_step;
+  d.cadist_step = s.cadist_step;
 }
 
 // ---- RyR transition draw (subroutine_cuda.c:332-363 and siblings) ----

@@ -59,13 +59,14 @@ struct rh_sim {
   double* d_partials = nullptr;
   double* d_out_wc = nullptr;
   double* d_out_ls = nullptr;
+  double* d_out_cd = nullptr;  // cadist records (record_cadist), per cell from cd_off
   double* d_diag = nullptr;
   rh_beat_stats* d_stats = nullptr;
   int64_t ls_rows_total = 0;
   // host mirror of each cell's clock (same IEEE additions as the device)
   std::vector<double> t_host;
   std::vector<char> active_host;
-  std::vector<long long> drained_wc, drained_ls, drained_st;
+  std::vector<long long> drained_wc, drained_ls, drained_st, drained_cd;
   // graphs keyed by (window length, output-step bitmask)
   std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
   // timing
@@ -216,6 +217,8 @@ StepArgs<R> make_args(rh_sim* s, const Lattice<R>& L, bool lattice_only) {
   a.partials = s->d_partials;
   a.out_wc = s->d_out_wc;
   a.out_ls = s->d_out_ls;
+  a.out_cd = s->d_out_cd;
+  a.cd_cap = s->opts.cadist_capacity;
   a.diag = (lattice_only || s->opts.keep_diagnostics) ? s->d_diag : nullptr;
   a.stats = s->d_stats;
   a.stats_cap = s->opts.stats_capacity;
@@ -403,6 +406,7 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   if (s->opts.output_capacity <= 0) s->opts.output_capacity = 64;
   if (s->opts.window_steps <= 0) s->opts.window_steps = 100;
   if (s->opts.stats_capacity <= 0) s->opts.stats_capacity = 64;
+  if (s->opts.cadist_capacity <= 0) s->opts.cadist_capacity = 8;
   if (!(s->opts.dt_ms > 0)) return fail(s, RH_ERR_ARG, "dt_ms must be positive");
   if (s->opts.precision != RH_FP64 && s->opts.precision != RH_MIXED)
     return fail(s, RH_ERR_ARG, "unknown precision %d", s->opts.precision);
@@ -411,6 +415,7 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   // layout
   int64_t off = 0;
   int64_t ls_off = 0;
+  int64_t cd_off = 0;
   for (int c = 0; c < ncells; ++c) {
     const rh_cell_params& p = cells[c];
     if (p.nx < 3 || p.ny < 3 || p.nz < 3 || p.nx > 4096 || p.ny > 4096 || p.nz > 4096)
@@ -436,6 +441,7 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     cc.seed = p.seed;
     cc.cell_id = p.cell_id;
     cc.ls_off = ls_off;
+    cc.cd_off = cd_off;
     cc.svica = ((0.666) * (1.2) * (p.ica_scale));
     cc.svncx = (2.5 * p.ncx_scale);
     double sviup = (1.0 + 0.75);
@@ -452,6 +458,8 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     cc.tend = p.nbeats * p.pcl_ms + 2100;
     off += (n64 + 31) & ~int64_t(31);
     ls_off += (int64_t)s->opts.output_capacity * cc.lx;
+    if (s->opts.record_cadist)
+      cd_off += (int64_t)s->opts.cadist_capacity * (2 + RH_CADIST_COLS * n64);
     s->max_n = std::max(s->max_n, cc.n);
     s->hcells.push_back(cc);
   }
@@ -535,6 +543,13 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   CK(cudaMalloc(&s->d_out_wc, sizeof(double) * RH_WHOLECELL_COLS * (size_t)ncells *
                                   s->opts.output_capacity));
   CK(cudaMalloc(&s->d_out_ls, sizeof(double) * RH_LINESCAN_COLS * (size_t)std::max<int64_t>(ls_off, 1)));
+  if (s->opts.record_cadist) {
+    if (cudaMalloc(&s->d_out_cd, sizeof(double) * (size_t)cd_off) != cudaSuccess) {
+      cudaGetLastError();
+      s->d_out_cd = nullptr;
+      return fail(s, RH_ERR_NOMEM, "cannot allocate %lld cadist values", (long long)cd_off);
+    }
+  }
   if (s->opts.track_stats)
     CK(cudaMalloc(&s->d_stats, sizeof(rh_beat_stats) * (size_t)ncells * s->opts.stats_capacity));
   // cells' basal state and membrane initial conditions
@@ -545,6 +560,7 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   s->drained_wc.assign(ncells, 0);
   s->drained_ls.assign(ncells, 0);
   s->drained_st.assign(ncells, 0);
+  s->drained_cd.assign(ncells, 0);
   for (int c = 0; c < ncells; ++c) {
     iv[c] = init_values(cells[c]);
     memset(&dyn[c], 0, sizeof(CellDyn));
@@ -586,6 +602,7 @@ int rh_destroy(rh_sim* s) {
   cudaFree(s->d_partials);
   cudaFree(s->d_out_wc);
   cudaFree(s->d_out_ls);
+  cudaFree(s->d_out_cd);
   cudaFree(s->d_diag);
   cudaFree(s->d_stats);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -942,6 +959,49 @@ int rh_drain_linescan(rh_sim* s, int32_t cell, double* rows, int32_t max_rec, in
   return RH_OK;
 }
 
+int rh_drain_cadist(rh_sim* s, int32_t cell, double* rec, int32_t max_rec, int32_t* nrec) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  if (!nrec || max_rec < 0 || (max_rec > 0 && !rec)) return RH_ERR_ARG;
+  *nrec = 0;
+  if (!s->d_out_cd) return fail(s, RH_ERR_ARG, "cadist records are off (run option record_cadist)");
+  CK(cudaSetDevice(s->device));
+  CellDyn d;
+  if ((r = read_dyn(s, cell, &d))) return r;
+  const int cap = s->opts.cadist_capacity;
+  const CellConst& cc = s->hcells[cell];
+  long long first = s->drained_cd[cell];
+  if (d.cd_count - first > cap) first = d.cd_count - cap;
+  const int cnt = (int)std::min<long long>(d.cd_count - first, max_rec);
+  const size_t len = 2 + (size_t)RH_CADIST_COLS * cc.n;
+  std::vector<double> dev(len);
+  for (int k = 0; k < cnt; ++k) {
+    const long long slot = (first + k) % cap;
+    CK(cudaMemcpy(dev.data(), s->d_out_cd + cc.cd_off + (size_t)slot * len, sizeof(double) * len,
+                  cudaMemcpyDeviceToHost));
+    // device rows are in CRU order (x fastest); the reference prints jx outer,
+    // jz inner (:1006-1008) and scales xinaca for print (:1009)
+    double* o = rec + (size_t)k * len;
+    o[0] = dev[0];
+    o[1] = dev[1];
+    for (int x = 0; x < cc.lx; ++x)
+      for (int y = 0; y < cc.ly; ++y)
+        for (int z = 0; z < cc.lz; ++z) {
+          const double* src = dev.data() + 2 + RH_CADIST_COLS * ((size_t)(z * cc.ly + y) * cc.lx + x);
+          double* dst = o + 2 + RH_CADIST_COLS * ((size_t)(x * cc.ly + y) * cc.lz + z);
+          dst[0] = src[0];
+          dst[1] = src[1];
+          dst[2] = src[2];
+          dst[3] = src[3];
+          dst[4] = src[4] / CM * 0.0965 * VS * 16120.;
+          dst[5] = src[5];
+        }
+  }
+  s->drained_cd[cell] = first + cnt;
+  *nrec = cnt;
+  return RH_OK;
+}
+
 int rh_drain_stats(rh_sim* s, int32_t cell, rh_beat_stats* out, int32_t max_rec, int32_t* nrec) {
   int r = check_cell(s, cell);
   if (r) return r;
@@ -1070,6 +1130,7 @@ int rh_restore(rh_sim* s, const char* path) {
     s->drained_wc[c] = dyn[c].out_count;
     s->drained_ls[c] = dyn[c].out_count;
     s->drained_st[c] = dyn[c].stats_count;
+    s->drained_cd[c] = dyn[c].cd_count;
   }
   return RH_OK;
 }
@@ -1109,6 +1170,7 @@ int rh_import_state(rh_sim* s, const void* host, size_t bytes) {
     s->drained_wc[c] = std::min(s->drained_wc[c], dyn[c].out_count);
     s->drained_ls[c] = std::min(s->drained_ls[c], dyn[c].out_count);
     s->drained_st[c] = std::min(s->drained_st[c], dyn[c].stats_count);
+    s->drained_cd[c] = std::min(s->drained_cd[c], dyn[c].cd_count);
   }
   CK(cudaStreamSynchronize(s->stream));
   return RH_OK;
@@ -1137,7 +1199,6 @@ int rh_autotune(rh_sim* s, int32_t steps, int32_t* tile, double* ms_per_step) {
   const std::vector<double> t0 = s->t_host;
   const std::vector<char> a0 = s->active_host;
   const int ts0 = s->ts;
-  const double dt = s->opts.dt_ms;
   double best = 1e300;
   int best_k = ts0;
   cudaEvent_t e0, e1;
@@ -1148,14 +1209,12 @@ int rh_autotune(rh_sim* s, int32_t steps, int32_t* tile, double* ms_per_step) {
     s->ts = k;
     cudaMemcpyAsync(s->arena, bk, s->arena_bytes, cudaMemcpyDeviceToDevice, s->stream);
     cudaMemcpyAsync(s->d_dyn, bk + s->arena_bytes, dyn_bytes, cudaMemcpyDeviceToDevice, s->stream);
-    std::vector<double> th = t0;
     cudaEventRecord(e0, s->stream);
     for (int i = 0; i < steps; ++i) {
-      bool out = false;
-      for (int c = 0; c < s->ncells; ++c)
-        if (a0[c] && out_step_host(th[c], dt)) out = true;
-      for (int c = 0; c < s->ncells; ++c) th[c] = th[c] + dt;
-      cudaError_t e = launch_one(s, out, false);
+      // the output-free kernel variant: the trial steps write no records, so
+      // records still waiting in the output rings are never overwritten (one
+      // step in 100 is an output step; its extra stores do not move the choice)
+      cudaError_t e = launch_one(s, false, false);
       if (e != cudaSuccess) {
         rc = fail(s, RH_ERR_CUDA, "autotune launch: %s", cudaGetErrorString(e));
         break;

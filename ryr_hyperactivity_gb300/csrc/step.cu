@@ -51,7 +51,7 @@ __device__ __forceinline__ R clamp0(R x) {
 // register allocation of the lattice code, which runs on every CTA.
 template <class R>
 __noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step, double* scratch,
-                                         int nw) {
+                                         int nw, bool cadist) {
   const int lane = threadIdx.x & 31;
   CellDyn* dyn = a.dyn + cell;
   const CellConst& cc = a.cells[cell];
@@ -82,7 +82,7 @@ __noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool ou
   rh_membrane m = dyn->m;
   const double dt = a.dt;
   // reduction (:447-456) and membrane model (:458-739), warp-parallel
-  double fm[3];
+  double fm[5];
   membrane_update_warp(m, dt, cc.pcl, cc.svikr, tot, cc.n, scratch, fm);
   uint32_t status = dyn->status;
   if (!isfinite(m.v) || !isfinite(m.xnai) || !isfinite(m.csubt) || !isfinite(m.xicatto) ||
@@ -102,6 +102,12 @@ __noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool ou
       long long slot = dyn->out_count % a.out_cap;
       double* w = a.out_wc + ((size_t)cell * a.out_cap + slot) * RH_WHOLECELL_COLS;
       wholecell_columns(w, osum, m, cc.n, dt);
+      if (cadist && a.out_cd) {  // record header: t and V of this output step (:1005)
+        double* h = a.out_cd + cc.cd_off + (dyn->cd_count % a.cd_cap) * (2 + 6 * (long long)cc.n);
+        h[0] = m.t;
+        h[1] = m.v;
+        dyn->cd_count += 1;
+      }
       if (a.stats) beat_on_output(dyn->bt, w);
       dyn->out_count += 1;
       m.sparksum = 0;  // :1074-1077
@@ -113,7 +119,7 @@ __noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool ou
   m.t = m.t + dt;  // :1083
   m.step += 1;
   StepCoef<double> kd;
-  const bool active = step_coef_warp(kd, m, cc, dt, fm[1], fm[2], scratch);
+  const bool active = step_coef_warp(kd, m, cc, dt, fm + 1, scratch);
   if (lane == 0) {
     StepCoef<float> kf;
     convert_coef(kf, kd);
@@ -177,7 +183,8 @@ struct TileSmem {
 struct TileHeader {
   int lx, ly, lz, nxf, nyf, tile_count, line_y, line_z;
   uint32_t seed, cell_id;
-  long long off, ls_off, step, slot;
+  long long off, ls_off, step, slot, cd_off, cd_slot;
+  int n;
   double t;
   int parity, done;
 };
@@ -270,6 +277,9 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       sh.step = d->m.step;
       sh.t = d->m.t;
       sh.slot = d->out_count % a.out_cap;
+      sh.n = c.n;
+      sh.cd_off = c.cd_off;
+      sh.cd_slot = a.out_cd ? d->cd_count % a.cd_cap : 0;
       sh.parity = d->parity;
       sh.done = d->done;
     }
@@ -281,6 +291,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   }
 
   const bool out_step = OUT && sk.output_step && !a.lattice_only;
+  const bool cadist_step = out_step && sk.cadist_step && a.out_cd != nullptr;
   const Lattice<R>& L = a.L;
   const int64_t S = L.stride;
   const int lx = sh.lx, ly = sh.ly, lz = sh.lz;
@@ -804,6 +815,15 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       }
       o[O_SPARK - P_STEP_END] = nspark;
       o[O_CIHIGH - P_STEP_END] = ci_high ? 1.0 : 0.0;
+      if (cadist_step) {  // cadist row (:1009), post-step values in this CRU's slot
+        double* r = a.out_cd + sh.cd_off + sh.cd_slot * (2 + 6 * (long long)sh.n) + 2 + 6 * (long long)q;
+        r[0] = (double)cinext2[g].x;
+        r[1] = (double)csn;
+        r[2] = (double)cp;
+        r[3] = (double)cjsr;
+        r[4] = (double)xinaca;  // scaled on the host as the reference prints it
+        r[5] = (double)xire;
+      }
       if (y == sh.line_y && z == sh.line_z) {  // linescan row (:967-989), post-step values
         const int64_t g0 = g;
         double* r = a.out_ls + ((size_t)sh.ls_off + (size_t)sh.slot * lx + x) * RH_LINESCAN_COLS;
@@ -884,7 +904,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   if (!__shfl_sync(0xffffffffu, last, 0)) return;
   // ---- last warp of the cell: whole-cell update ----
   __threadfence();
-  if (!a.lattice_only) cell_update<R>(a, cell, out_step, s_cu, NW);
+  if (!a.lattice_only) cell_update<R>(a, cell, out_step, s_cu, NW, cadist_step);
   __syncwarp();
   if (lane < 6) a.dyn[cell].acc[lane] = 0ull;  // the next step starts from zero
   if (lane == 0) {

@@ -120,6 +120,15 @@ class Simulator:
                                           max_rec, C.byref(n)))
         return a[: n.value].copy()
 
+    def drain_cadist(self, cell: int = 0, max_rec: int = 64) -> np.ndarray:
+        """cadist records (run option record_cadist=1), one row each: t, V,
+        then 6 values per interior CRU in the reference's order."""
+        a = np.zeros((max_rec, 2 + 6 * self.n[cell]))
+        n = C.c_int32()
+        self._ck(self.L.rh_drain_cadist(self.h, cell, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                        max_rec, C.byref(n)))
+        return a[: n.value].copy()
+
     def drain_stats(self, cell: int = 0, max_rec: int = 256) -> list[dict]:
         arr = (BeatStats * max_rec)()
         n = C.c_int32()

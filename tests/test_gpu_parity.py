@@ -266,3 +266,104 @@ def test_cell_groups_give_identical_results():
                     np.testing.assert_array_equal(st[c][k], st0[c][k], err_msg=f"{precision} {k}")
                 assert m[c].v == m0[c].v and m[c].xnai == m0[c].xnai and m[c].t == m0[c].t
                 np.testing.assert_array_equal(wc[c], wc0[c])
+
+
+def _small_il():
+    """The reference's small_il fixture cell (12x9x7, PCL 1000 ms, lqt/iso2
+    build, curand seed 18) and its recorded cadist run."""
+    import json
+    gold = os.path.join(os.path.dirname(__file__), "golden")
+    spec = json.load(open(os.path.join(gold, "ref_full_runs.json")))["small_il_cd"]
+    a = spec["args"]
+    p = cell_params(clamp_mv=a[0], cjsr_basal=a[1], ncx_scale=a[2], ku=a[3], r1=a[4], kb=a[5],
+                    ica_scale=a[6], ku2=a[7], seed=spec["seed"], **spec["cell"])
+    return p, spec, a
+
+
+def test_fp64_cadist_matches_reference_file():
+    """cadist records (the outputcadist build, cuda_Cell_Detailed.cu:1001-1013)
+    through the C ABI: equal to the oracle's within 1e-9 and, printed as the
+    reference prints them, the same bytes as the reference program's own
+    cadist_ file (sha256 of the fixture run)."""
+    import hashlib
+    p, spec, _ = _small_il()
+    ref = O.Oracle(p).run_cadist(spec["steps"])
+    recs = []
+    with Simulator(p, precision="fp64", record_cadist=1, cadist_capacity=4) as sim:
+        done = 0
+        while done < spec["steps"]:  # drained every 500 steps (at most 3 records)
+            k = min(500, spec["steps"] - done)
+            sim.run_steps(k)
+            done += k
+            recs.extend(sim.drain_cadist(0))
+    assert len(recs) == len(ref) == spec["cadist_records"]
+    for r, w in zip(recs, ref):
+        assert r[0] == w[0]  # the same clock, bit for bit
+        np.testing.assert_allclose(r, w, rtol=1e-9, atol=1e-12)
+    text = O.cadist_text(recs)
+    assert hashlib.sha256(text.encode()).hexdigest() == spec["cadist_sha256"]
+
+
+def test_cadist_batched_cells_groups_and_period_gap():
+    """Each cell's cadist records land in its own ring: two cells of different
+    size on two streams, one with PCL 520 ms so the 500 ms recording window
+    closes (no records in 500..515 ms) and reopens at the next period."""
+    p0, _, _ = _small_il()
+    cells = [p0, cell_params(nx=5, ny=4, nz=4, nbeats=2, pcl_ms=520.0, seed=5, cell_id=1)]
+    nsteps = 21000
+    refs = [O.Oracle(p).run_cadist(nsteps) for p in cells]
+    got = [[], []]
+    with Simulator(cells, precision="fp64", record_cadist=1, cadist_capacity=16,
+                   cell_groups=2) as sim:
+        assert sim.num_groups() == 2
+        done = 0
+        while done < nsteps:
+            k = min(2000, nsteps - done)  # at most 10 records per cell between drains
+            sim.run_steps(k)
+            done += k
+            for c in range(2):
+                got[c].extend(sim.drain_cadist(c))
+    for c in range(2):
+        assert len(got[c]) == len(refs[c]), c
+        np.testing.assert_allclose(np.array(got[c]), np.array(refs[c]), rtol=1e-9, atol=1e-12)
+    t1 = np.array([r[0] for r in got[1]])
+    assert not np.any((t1 > 496) & (t1 < 519)) and np.any(t1 > 519)
+
+
+def test_cadist_mixed_precision_records():
+    """The mixed path writes the same records at the same times; its lattice
+    values are the FP32 state (ci, cs, cjsr within 1e-4 relative of FP64
+    before the first stimulus)."""
+    p, spec, _ = _small_il()
+    out = {}
+    for precision in ("fp64", "mixed"):
+        with Simulator(p, precision=precision, record_cadist=1, cadist_capacity=16) as sim:
+            sim.run_steps(spec["steps"])
+            out[precision] = sim.drain_cadist(0)
+    a, b = out["fp64"], out["mixed"]
+    assert a.shape == b.shape == (spec["cadist_records"], 2 + 6 * sim.n[0])
+    np.testing.assert_array_equal(a[:, 0], b[:, 0])
+    ra = a[:, 2:].reshape(len(a), -1, 6)
+    rb = b[:, 2:].reshape(len(b), -1, 6)
+    for col in (0, 1, 3):
+        np.testing.assert_allclose(rb[:, :, col], ra[:, :, col], rtol=1e-4)
+
+
+def test_cli_cadist_file_is_the_reference_file():
+    """The drop-in program with --cadist writes the reference's cadist_ file:
+    the same sha256 as the reference program built with outputcadist."""
+    import hashlib
+    exe = os.path.join(os.path.dirname(os.path.dirname(__file__)), "ryr_hyperactivity_gb300",
+                       "bin", "cuda_Cell_Detailed")
+    p, spec, a = _small_il()
+    c = spec["cell"]
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run([exe, "0", "cd"] + [str(x) for x in a] +
+                       ["--nx", str(c["nx"]), "--ny", str(c["ny"]), "--nz", str(c["nz"]),
+                        "--nbeats", str(c["nbeats"]), "--pcl", str(c["pcl_ms"]),
+                        "--lqt", str(c["lqt"]), "--iso2", str(c["iso2"]), "--cadist",
+                        "--max-steps", str(spec["steps"])],
+                       cwd=d, check=True, capture_output=True)
+        text = open(os.path.join(d, "cadist_cd")).read()
+    assert text.count("header") == spec["cadist_records"]
+    assert hashlib.sha256(text.encode()).hexdigest() == spec["cadist_sha256"]
