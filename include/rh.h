@@ -68,6 +68,20 @@ extern "C" {
 #define RH_LINESCAN_COLS 22
 #define RH_CADIST_COLS 6 /* per interior CRU; a record adds t and V */
 
+/* Membrane-voltage protocols (the reference's compile-time protocol switches,
+ * cuda_Cell_Detailed.cu:34, :54-61, :733-773).  The voltage the model computes
+ * is replaced after each step by the protocol's value, except for PACED and
+ * NOPACING, which only differ in the stimulus. */
+#define RH_PROTO_PACED 0           /* default build: 80 uA/uF for 1 ms at t = 100 + k*PCL (:689) */
+#define RH_PROTO_NOPACING 1        /* -Dnopacing: no stimulus (:694-696) */
+#define RH_PROTO_VCLAMP 2          /* -Dvclamp: -86 mV, clamp_mv after t > 100 ms (:733-739) */
+#define RH_PROTO_BROWN_VCLAMP 3    /* -Dbrownvclamp: -86/-10/10/-30/-86 mV steps at 4000, 4200,
+                                      6200, 7200 ms (:741-752) */
+#define RH_PROTO_AP_CLAMP 4        /* -Dapclamp: V from a recorded waveform of PCL/dt samples,
+                                      repeated every PCL (:383-395, :754-757); the waveform is
+                                      given with rh_set_ap_clamp */
+#define RH_PROTO_LINEAR_AP_CLAMP 5 /* -Dlinearapclamp: piecewise-linear AP (:758-773) */
+
 /* Parameters of one cell.  argv[k] refers to the reference command line
  * (cuda_Cell_Detailed <dev> <name> a3 .. a10). */
 typedef struct {
@@ -92,6 +106,11 @@ typedef struct {
   uint32_t cell_id;     /* Philox key word 1 */
   int32_t linescan_jz;  /* z plane of the linescan; -1 = reference's 5 (:972),
                            clamped to nz-2 when the lattice is thinner */
+  int32_t protocol;     /* RH_PROTO_* (default RH_PROTO_PACED) */
+  int32_t perm;         /* -Dperm (:35): permeabilised cell.  No LCC or NCX flux, no
+                           stimulus, [Ca] 0.3 uM held at the lattice faces and
+                           leaking into the submembrane space (:1409-1411), initial
+                           [Ca]i 0.3 uM and JSR 900 uM (argv[4] unused, :87-93) */
 } rh_cell_params;
 
 /* Run-wide options. */
@@ -184,6 +203,12 @@ int rh_run_to_end(rh_sim* sim);
  * with the cell's current v, t and [Na]i; no reduction, no V update, t does
  * not advance.  For single-step parity checks. */
 int rh_lattice_step(rh_sim* sim);
+
+/* Waveform of an RH_PROTO_AP_CLAMP cell: n = (int)(pcl_ms/dt + 0.1) voltages
+ * (mV), sample k applied at the steps whose (int)(t/dt + 0.1) is k modulo n
+ * (the reference reads them from v_1000.txt, :383-395).  Copied; must be set
+ * before such a cell runs (rh_run_steps fails with RH_ERR_STATE otherwise). */
+int rh_set_ap_clamp(rh_sim* sim, int32_t cell, const double* v_mV, int64_t n);
 
 /* Number of cells / interior CRUs of a cell. */
 int rh_num_cells(const rh_sim* sim, int32_t* ncells);

@@ -59,6 +59,14 @@ declare -A VARIANTS=(
   [default_il]="-Diso2 -Dlqt -DREF_LINESCAN_JZ=5"
   # small_il with the reference's cadist_ writer enabled (#define outputcadist)
   [small_il_cd]="-Dnx=12 -Dny=9 -Dnz=7 -Dnbeat=1 -Dtperid=1000.0 -DREF_LINESCAN_JZ=5 -Diso2 -Dlqt -Doutputcadist"
+  # the voltage protocols and cell preparations of the reference's build
+  # switches (:34-35, :54-61), each on a small lattice
+  [vclamp]="-Dnx=12 -Dny=8 -Dnz=5 -Dnbeat=1 -Dtperid=400.0 -DREF_LINESCAN_JZ=2 -Dvclamp"
+  [brownvclamp]="-Dnx=6 -Dny=5 -Dnz=4 -Dnbeat=2 -Dtperid=3000.0 -DREF_LINESCAN_JZ=2 -Dbrownvclamp"
+  [apclamp]="-Dnx=10 -Dny=6 -Dnz=5 -Dnbeat=2 -Dtperid=200.0 -DREF_LINESCAN_JZ=2 -Diso2 -Dlqt -Dapclamp"
+  [linearapclamp]="-Dnx=12 -Dny=8 -Dnz=5 -Dnbeat=1 -Dtperid=1000.0 -DREF_LINESCAN_JZ=2 -Dlinearapclamp"
+  [nopacing]="-Dnx=12 -Dny=8 -Dnz=5 -Dnbeat=1 -Dtperid=400.0 -DREF_LINESCAN_JZ=2 -Diso2 -Dlqt -Dnopacing"
+  [perm]="-Dnx=12 -Dny=9 -Dnz=6 -Dnbeat=1 -Dtperid=1000.0 -DREF_LINESCAN_JZ=3 -Dperm"
 )
 want=("$@")
 if [ ${#want[@]} -eq 0 ]; then want=("${!VARIANTS[@]}"); fi

@@ -63,6 +63,8 @@ def lib() -> C.CDLL:
         L.orc_last_linescan.restype = C.c_int32
         L.orc_last_cadist.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_last_cadist.restype = C.c_int32
+        L.orc_set_ap_clamp.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int64]
+        L.orc_set_ap_clamp.restype = C.c_int32
         L.orc_protocol_done.argtypes = [C.c_void_p]
         L.orc_protocol_done.restype = C.c_int32
         L.orc_status.argtypes = [C.c_void_p]
@@ -114,7 +116,16 @@ class Oracle:
             self.h = None
 
     def step(self) -> bool:
-        return bool(self.L.orc_step(self.h))
+        r = self.L.orc_step(self.h)
+        if r < 0:
+            raise RuntimeError("AP-clamp waveform not set")
+        return bool(r)
+
+    def set_ap_clamp(self, v) -> None:
+        """Waveform of an AP-clamp cell: (int)(pcl/dt + 0.1) voltages (mV)."""
+        a = np.ascontiguousarray(v, np.float64)
+        if self.L.orc_set_ap_clamp(self.h, _dptr(a), len(a)) != 0:
+            raise ValueError("orc_set_ap_clamp rejected the waveform")
 
     def lattice_step(self) -> None:
         self.L.orc_lattice_step(self.h)
@@ -151,7 +162,8 @@ class Oracle:
         for _ in range(int(nsteps)):
             if self.done:
                 break
-            self.L.orc_step(self.h)
+            if self.L.orc_step(self.h) < 0:
+                raise RuntimeError("AP-clamp waveform not set")
             if self.L.orc_last_cadist(self.h, _dptr(buf)):
                 recs.append(buf.copy())
         return recs

@@ -47,6 +47,8 @@
 #define FRT (96.485 / 8.314 / 308.0) /* :83 */
 #define XI 0.7                   /* :84 */
 #define CI_BASAL 0.0944          /* :91 */
+#define PERM_CI_BASAL 0.3        /* :88, the perm build */
+#define PERM_CJSR_BASAL 900      /* :89, the perm build */
 #define VS 0.025                 /* :95 */
 #define ICAGAMMA 0.5             /* :99 */
 #define CM 45                    /* :100 */
@@ -153,6 +155,8 @@ struct orc_sim {
   double* ls; /* (nx-2) x 22 */
   double* cd; /* cadist record: t, v, then 6 values per interior CRU */
   int cd_valid;
+  double* apv; /* AP-clamp waveform (orc_set_ap_clamp), napv samples */
+  int napv;
 };
 
 static inline int opos(const orc_sim* s, int i, int j, int k) {
@@ -469,11 +473,14 @@ static int lcc_next(int st, double u, double dt, const lcc_rates* r) {
 
 /* Basal state of every CRU incl. ghosts (cuda_Cell_Detailed.cu:1108-1182). */
 static void init_lattice(orc_sim* s) {
-  double cjsr_b = s->p.tapsi ? 10 : s->p.cjsr_basal; /* :1118-1120 */
+  /* ci_basal and cjsr_basal are fixed in the perm build (:87-92); tapsi then
+   * overrides the load (:1118-1120) */
+  const double CI_B = s->p.perm ? PERM_CI_BASAL : CI_BASAL;
+  double cjsr_b = s->p.tapsi ? 10 : (s->p.perm ? PERM_CJSR_BASAL : s->p.cjsr_basal);
   for (int ac = 0; ac < s->ntot; ++ac) {
-    s->cp[ac] = CI_BASAL;
-    s->cs[0][ac] = CI_BASAL;
-    s->cs[1][ac] = CI_BASAL;
+    s->cp[ac] = CI_B;
+    s->cs[0][ac] = CI_B;
+    s->cs[1][ac] = CI_B;
     s->cjsr[ac] = cjsr_b;
     s->cjsrb[ac] = csqn_bound_ss(cjsr_b);
     s->nspark[ac] = 0;
@@ -485,24 +492,24 @@ static void init_lattice(orc_sim* s) {
     s->xicat[ac] = 0;
     for (int ii = 0; ii < 8; ++ii) {
       int a8 = ac * 8 + ii;
-      s->ci[0][a8] = CI_BASAL;
-      s->ci[1][a8] = CI_BASAL;
+      s->ci[0][a8] = CI_B;
+      s->ci[1][a8] = CI_B;
       s->cnsr[0][a8] = cjsr_b;
       s->cnsr[1][a8] = cjsr_b;
-      s->catf[a8] = KTFON * CI_BASAL * BTF / (KTFON * CI_BASAL + KTFOFF);
-      s->cats[a8] = KTSON * CI_BASAL * BTS / (KTSON * CI_BASAL + KTSOFF);
-      s->cacal[a8] = KCALON * CI_BASAL * BCAL / (KCALON * CI_BASAL + KCALOFF);
-      s->cadye[a8] = KDYEON * CI_BASAL * BDYE / (KDYEON * CI_BASAL + KDYEOFF);
-      s->casr[a8] = KSRON * CI_BASAL * BSR / (KSRON * CI_BASAL + KSROFF);
+      s->catf[a8] = KTFON * CI_B * BTF / (KTFON * CI_B + KTFOFF);
+      s->cats[a8] = KTSON * CI_B * BTS / (KTSON * CI_B + KTSOFF);
+      s->cacal[a8] = KCALON * CI_B * BCAL / (KCALON * CI_B + KCALOFF);
+      s->cadye[a8] = KDYEON * CI_B * BDYE / (KDYEON * CI_B + KDYEOFF);
+      s->casr[a8] = KSRON * CI_B * BSR / (KSRON * CI_B + KSROFF);
       s->camyo[a8] = 3.;
       s->mgmyo[a8] = 136.209996;
       s->xiup[a8] = 0;
       s->xileak[a8] = 0;
     }
-    s->casar[ac] = KSARON * CI_BASAL * BSAR / (KSARON * CI_BASAL + KSAROFF);
-    s->casarh[ac] = KSARHON * CI_BASAL * BSARH / (KSARHON * CI_BASAL + KSARHOFF);
-    s->casarj[ac] = KSARON * CI_BASAL * BSAR / (KSARON * CI_BASAL + KSAROFF);
-    s->casarhj[ac] = KSARHON * CI_BASAL * BSARH / (KSARHON * CI_BASAL + KSARHOFF);
+    s->casar[ac] = KSARON * CI_B * BSAR / (KSARON * CI_B + KSAROFF);
+    s->casarh[ac] = KSARHON * CI_B * BSARH / (KSARHON * CI_B + KSARHOFF);
+    s->casarj[ac] = KSARON * CI_B * BSAR / (KSARON * CI_B + KSAROFF);
+    s->casarhj[ac] = KSARHON * CI_B * BSARH / (KSARHON * CI_B + KSARHOFF);
     for (int ll = 0; ll < 8; ++ll) s->lcc[ac * 8 + ll] = (ll < SVNCP) ? 3 : 16;
     double roo2 = RATEDIMER / (1.0 + pow(KDIMER / (cjsr_b), HILLDIMER));
     double aub = (-1.0 + sqrt(1.0 + 8.0 * CSQBERS * roo2)) / (4.0 * roo2 * CSQBERS) / TAUB;
@@ -538,20 +545,23 @@ static void update_cru(orc_sim* s, int i, int j, int k, double v, double t, doub
     s->nspark[ac] = 0;
     s->nl[ac] = 0;
   }
-  /* LCC channels (:1248-1263) */
-  double cpx = (s->cp[ac] + cs[ac] * ICAGAMMA) / (1 + ICAGAMMA);
-  lcc_rates lr = lcc_rates_at(cpx, v, s->p.iso2);
-  int nlcp = 0;
-  for (int ll = 0; ll < 8 && s->lcc[ac * 8 + ll] < 16; ll++) {
-    double u = rh_uniform_double(&rng);
-    int jj = lcc_next(s->lcc[ac * 8 + ll], u, dt, &lr);
-    s->lcc[ac * 8 + ll] = jj;
-    if (jj == 0) {
-      ++s->nl[ac];
-      ++nlcp;
+  /* LCC channels (:1248-1263); none in the perm build (:1249) */
+  double icat1 = 0;
+  if (!s->p.perm) {
+    double cpx = (s->cp[ac] + cs[ac] * ICAGAMMA) / (1 + ICAGAMMA);
+    lcc_rates lr = lcc_rates_at(cpx, v, s->p.iso2);
+    int nlcp = 0;
+    for (int ll = 0; ll < 8 && s->lcc[ac * 8 + ll] < 16; ll++) {
+      double u = rh_uniform_double(&rng);
+      int jj = lcc_next(s->lcc[ac * 8 + ll], u, dt, &lr);
+      s->lcc[ac * 8 + ll] = jj;
+      if (jj == 0) {
+        ++s->nl[ac];
+        ++nlcp;
+      }
     }
+    icat1 = s->svica * (double)(nlcp)*lcc_flux(v, cpx, s->cao);
   }
-  double icat1 = s->svica * (double)(nlcp)*lcc_flux(v, cpx, s->cao);
   const double pmca = 0, bcgcur = 0; /* :1265-1269, both zero in the default build */
   s->xicat[ac] = icat1 + pmca + bcgcur * (VS / VP);
 
@@ -564,8 +574,10 @@ static void update_cru(orc_sim* s, int i, int j, int k, double v, double t, doub
   s->xire[ac] = jsr_release(s->po[ac], s->cjsr[ac], s->cp[ac]) / randomi;
   if (s->xire[ac] < 0) s->xire[ac] = 0;
 
-  /* NCX (:1296) */
-  s->xinaca[ac] = s->svncx * 1.0 * ncx_flux(cs[ac] / 1000.0, v, xnai, &s->ancx[ac], dt, s->cao);
+  /* NCX (:1296); not computed in the perm build (:1294-1300), where
+   * xinaca keeps its zero-filled start and Ancx its initial value */
+  if (!s->p.perm)
+    s->xinaca[ac] = s->svncx * 1.0 * ncx_flux(cs[ac] / 1000.0, v, xnai, &s->ancx[ac], dt, s->cao);
 
   /* SERCA and leak per sub-voxel (:1305-1308) */
   for (int ii = 0; ii < 8; ++ii) {
@@ -652,6 +664,7 @@ static void update_cru(orc_sim* s, int i, int j, int k, double v, double t, doub
     double csbuffers = (buffer_rate(KSARON, KSAROFF, BSAR, s->casar[ac], csnext[ac], dth) +
                         buffer_rate(KSARHON, KSARHOFF, BSARH, s->casarh[ac], csnext[ac], dth));
     double csdiff = (cs[kz_up] + cs[kz_dn] - 2 * cs[ac]) / (TAUST);
+    if (s->p.perm) csdiff += (PERM_CI_BASAL - csnext[ac]) / 5; /* :1409-1411 */
     double dotcs = VP / VS * (s->cp[ac] - csnext[ac]) / (TAUPS) - ICAGAMMA * icat1 * VP / VS +
                    s->xinaca[ac] - (cs[ac] - ci[ac * 8]) / TAUSI / 2. -
                    (cs[ac] - ci[ac * 8 + 1]) / TAUSI / 2. + csdiff - csbuffers - bcgcur;
@@ -680,8 +693,10 @@ static void update_cru(orc_sim* s, int i, int j, int k, double v, double t, doub
 
 /* Zero-flux boundaries: ghost faces copy the facing interior sub-voxels
  * (cuda_Cell_Detailed.cu:1603-1652).  Only face ghosts are written, which are
- * the only ghosts the stencil reads. */
+ * the only ghosts the stencil reads.  The perm build copies only cnsr
+ * (:1653-1689): the ci and cs ghosts keep their initial bath value. */
 static void apply_ghost_faces(orc_sim* s) {
+  const int perm = s->p.perm;
   double* ci = s->ci[1 - s->cur];
   double* cn = s->cnsr[1 - s->cur];
   double* cs = s->cs[1 - s->cur];
@@ -691,11 +706,11 @@ static void apply_ghost_faces(orc_sim* s) {
       int g0 = opos(s, 0, j, k) * 8, i1 = opos(s, 1, j, k) * 8;
       int g1 = opos(s, nx - 1, j, k) * 8, i2 = opos(s, nx - 2, j, k) * 8;
       for (int ii = 4; ii < 8; ++ii) {
-        ci[g0 + ii] = ci[i1 + ii - 4];
+        if (!perm) ci[g0 + ii] = ci[i1 + ii - 4];
         cn[g0 + ii] = cn[i1 + ii - 4];
       }
       for (int ii = 0; ii < 4; ++ii) {
-        ci[g1 + ii] = ci[i2 + ii + 4];
+        if (!perm) ci[g1 + ii] = ci[i2 + ii + 4];
         cn[g1 + ii] = cn[i2 + ii + 4];
       }
     }
@@ -704,14 +719,18 @@ static void apply_ghost_faces(orc_sim* s) {
       int g0 = opos(s, i, 0, k) * 8, i1 = opos(s, i, 1, k) * 8;
       int g1 = opos(s, i, ny - 1, k) * 8, i2 = opos(s, i, ny - 2, k) * 8;
       for (int ii = 2; ii < 8; ii += 4) {
-        ci[g0 + ii] = ci[i1 + ii - 2];
-        ci[g0 + ii + 1] = ci[i1 + ii - 1];
+        if (!perm) {
+          ci[g0 + ii] = ci[i1 + ii - 2];
+          ci[g0 + ii + 1] = ci[i1 + ii - 1];
+        }
         cn[g0 + ii] = cn[i1 + ii - 2];
         cn[g0 + ii + 1] = cn[i1 + ii - 1];
       }
       for (int ii = 0; ii < 8; ii += 4) {
-        ci[g1 + ii] = ci[i2 + ii + 2];
-        ci[g1 + ii + 1] = ci[i2 + ii + 3];
+        if (!perm) {
+          ci[g1 + ii] = ci[i2 + ii + 2];
+          ci[g1 + ii + 1] = ci[i2 + ii + 3];
+        }
         cn[g1 + ii] = cn[i2 + ii + 2];
         cn[g1 + ii + 1] = cn[i2 + ii + 3];
       }
@@ -721,15 +740,17 @@ static void apply_ghost_faces(orc_sim* s) {
       int g0 = opos(s, i, j, 0), i1 = opos(s, i, j, 1);
       int g1 = opos(s, i, j, nz - 1), i2 = opos(s, i, j, nz - 2);
       for (int ii = 1; ii < 8; ii += 2) {
-        ci[g0 * 8 + ii] = ci[i1 * 8 + ii - 1];
+        if (!perm) ci[g0 * 8 + ii] = ci[i1 * 8 + ii - 1];
         cn[g0 * 8 + ii] = cn[i1 * 8 + ii - 1];
       }
       for (int ii = 0; ii < 8; ii += 2) {
-        ci[g1 * 8 + ii] = ci[i2 * 8 + ii + 1];
+        if (!perm) ci[g1 * 8 + ii] = ci[i2 * 8 + ii + 1];
         cn[g1 * 8 + ii] = cn[i2 * 8 + ii + 1];
       }
-      cs[g0] = cs[i1];
-      cs[g1] = cs[i2];
+      if (!perm) {
+        cs[g0] = cs[i1];
+        cs[g1] = cs[i2];
+      }
     }
 }
 
@@ -871,10 +892,11 @@ static void membrane_update(orc_sim* s) {
   double fnak = 1.00 / (1.0 + 0.1245 * exp(-0.1 * v * FRT) + 0.0365 * sigma * exp(-v * FRT));
   double xinak =
       svnak * xibarnak * fnak * (1.0 / (1.0 + pow((xkmnai / xnai), hh))) * xko / (xko + xkmko);
-  /* stimulus (:689-692) */
+  /* stimulus (:689-692); none in the nopacing and perm builds (:694-699) */
   double stim;
   if (fmod(t + tperid - 100, tperid) < 1.0) stim = 80.0;
   else stim = 0.0;
+  if (s->p.protocol == RH_PROTO_NOPACING || s->p.perm) stim = 0.0;
   /* [Na]i and V (:701-738) */
   double wcainv = 1.0 / 50.0;
   double conv = 0.18 * 12500;
@@ -887,6 +909,34 @@ static void membrane_update(orc_sim* s) {
                  1 * m->xicatto + xinak) +
                stim;
   m->v = v + dvh * dt;
+  /* voltage protocols (:733-773): the clamp replaces the integrated V */
+  switch (s->p.protocol) {
+    case RH_PROTO_VCLAMP: /* :733-739 */
+      m->v = -86;
+      if (t > 100) m->v = s->p.clamp_mv;
+      break;
+    case RH_PROTO_BROWN_VCLAMP: /* :741-752 */
+      if (t < 4000) m->v = -86;
+      else if (t < 4200) m->v = -10;
+      else if (t < 6200) m->v = 10;
+      else if (t < 7200) m->v = -30;
+      else m->v = -86;
+      break;
+    case RH_PROTO_AP_CLAMP: /* :754-757 */
+      m->v = s->apv[((int)(t / dt + 0.1)) % ((int)(tperid / dt + 0.1))];
+      break;
+    case RH_PROTO_LINEAR_AP_CLAMP: /* :758-773 */
+      if (t < 100) m->v = -86;
+      else if (t < 101.865) m->v = 68 * (t - 100) - 80;
+      else if (t < 119.1) m->v = -(t - 100) + 48;
+      else if (t < 138.9) m->v = 27 + 0.1 * (t - 100);
+      else if (t < 364.43) m->v = 43 - (t - 100) / 3.2;
+      else if (t < 395.43) m->v = -1.5 * (t - 100) + 357;
+      else m->v = -86;
+      break;
+    default:
+      break;
+  }
   m->out_ica += m->xicatto; /* :774-776 */
   m->out_ncx += m->xinacato;
   m->out_ina += xina;
@@ -1114,6 +1164,7 @@ static void output_record(orc_sim* s) {
 }
 
 int orc_step(orc_sim* s) {
+  if (s->p.protocol == RH_PROTO_AP_CLAMP && !s->apv) return -1; /* no waveform */
   orc_lattice_step(s);
   s->m.step += 1;
   wholecell_reduce(s);
@@ -1132,13 +1183,27 @@ int orc_step(orc_sim* s) {
 
 int32_t orc_protocol_done(const orc_sim* s) { return !(s->m.t < s->tend); }
 
+int32_t orc_set_ap_clamp(orc_sim* s, const double* v, int64_t n) {
+  const int need = (int)(s->p.pcl_ms / s->dt + 0.1); /* numsteps, :384 */
+  if (s->p.protocol != RH_PROTO_AP_CLAMP || !v || n != need) return -1;
+  double* w = (double*)malloc(sizeof(double) * (size_t)n);
+  if (!w) return -1;
+  memcpy(w, v, sizeof(double) * (size_t)n);
+  free(s->apv);
+  s->apv = w;
+  s->napv = need;
+  return 0;
+}
+
 int64_t orc_run(orc_sim* s, int64_t nsteps, double* wholecell, int32_t max_rec, int32_t* nrec,
                 double* linescan, int32_t max_blocks, int32_t* nblocks) {
   int64_t done = 0;
   int32_t nr = 0, nb = 0;
   const int lrows = s->nx - 2;
   while (done < nsteps && s->m.t < s->tend) { /* :399 */
-    if (orc_step(s)) {
+    const int out = orc_step(s);
+    if (out < 0) break;
+    if (out) {
       if (wholecell && nr < max_rec)
         memcpy(wholecell + (size_t)nr * RH_WHOLECELL_COLS, s->wc, sizeof(s->wc));
       if (nr < max_rec) nr++;
@@ -1162,6 +1227,7 @@ int64_t orc_run_traced(orc_sim* s, int64_t nsteps, double* t_out, double* v_out,
   while (done < nsteps && s->m.t < s->tend) {
     double t0 = s->m.t;
     int out = orc_step(s);
+    if (out < 0) break;
     if (t_out) t_out[done] = t0;
     if (v_out) v_out[done] = s->m.v;
     if (out && wholecell && nr < max_rec) {
@@ -1248,6 +1314,7 @@ void orc_destroy(orc_sim* s) {
                   s->cats, s->cacal, s->casr, s->camyo, s->mgmyo, s->cadye, s->ci[0], s->ci[1],
                   s->cnsr[0], s->cnsr[1], s->cs[0], s->cs[1], s->ls, s->cd};
   for (size_t q = 0; q < sizeof(dp) / sizeof(dp[0]); ++q) free(dp[q]);
+  free(s->apv);
   int* ip[] = {s->lcc, s->nl, s->nou, s->ncu, s->nob, s->ncb, s->nspark};
   for (size_t q = 0; q < sizeof(ip) / sizeof(ip[0]); ++q) free(ip[q]);
   free(s);

@@ -35,7 +35,8 @@ int orc_get_threads(void);
 
 /* One iteration of the reference's time loop (:399-1085): lattice update,
  * whole-cell reduction, membrane model, output bookkeeping, t += dt.
- * Returns 1 when this step produced an output record. */
+ * Returns 1 when this step produced an output record, -1 (nothing done) for an
+ * AP-clamp cell without its waveform. */
 int orc_step(orc_sim* s);
 
 /* Runs `nsteps` iterations (or until the protocol ends) and copies each
@@ -67,6 +68,9 @@ int32_t orc_last_linescan(const orc_sim* s, double* rows);
 int32_t orc_last_cadist(const orc_sim* s, double* rec);
 
 int32_t orc_protocol_done(const orc_sim* s);
+/* Waveform of an RH_PROTO_AP_CLAMP cell: (int)(pcl/dt + 0.1) voltages, the
+ * values the reference reads from v_1000.txt (:383-395).  0 on success. */
+int32_t orc_set_ap_clamp(orc_sim* s, const double* v, int64_t n);
 uint32_t orc_status(const orc_sim* s);
 int32_t orc_interior(const orc_sim* s);
 

@@ -20,6 +20,17 @@ RH_STATUS_RATE_CAP = 0x10
 RH_STATUS_TIMEOUT = 0x20
 WHOLECELL_COLS = 45
 LINESCAN_COLS = 22
+CADIST_COLS = 6
+RH_PROTO_PACED = 0
+RH_PROTO_NOPACING = 1
+RH_PROTO_VCLAMP = 2
+RH_PROTO_BROWN_VCLAMP = 3
+RH_PROTO_AP_CLAMP = 4
+RH_PROTO_LINEAR_AP_CLAMP = 5
+# protocol names as the reference's build switches spell them
+PROTOCOLS = {"paced": RH_PROTO_PACED, "nopacing": RH_PROTO_NOPACING, "vclamp": RH_PROTO_VCLAMP,
+             "brownvclamp": RH_PROTO_BROWN_VCLAMP, "apclamp": RH_PROTO_AP_CLAMP,
+             "linearapclamp": RH_PROTO_LINEAR_AP_CLAMP}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -44,6 +55,8 @@ class CellParams(C.Structure):
         ("seed", C.c_uint32),
         ("cell_id", C.c_uint32),
         ("linescan_jz", C.c_int32),
+        ("protocol", C.c_int32),
+        ("perm", C.c_int32),
     ]
 
 
@@ -115,8 +128,11 @@ def cell_params(**kw) -> CellParams:
     lattice, make-il build) overridden by keyword arguments."""
     d = dict(nx=64, ny=28, nz=12, nbeats=7, pcl_ms=4000.0, clamp_mv=1.0, cjsr_basal=740.0,
              ncx_scale=1.0, ku=3.333, r1=0.0, kb=18.0, ica_scale=0.7, ku2=1.0, ikr_scale=1.0,
-             cao_mM=1.8, lqt=1, iso2=1, tapsi=0, seed=18, cell_id=0, linescan_jz=-1)
+             cao_mM=1.8, lqt=1, iso2=1, tapsi=0, seed=18, cell_id=0, linescan_jz=-1,
+             protocol=RH_PROTO_PACED, perm=0)
     d.update(kw)
+    if isinstance(d["protocol"], str):  # a build-switch name, e.g. "vclamp"
+        d["protocol"] = PROTOCOLS[d["protocol"]]
     p = CellParams()
     for k, v in d.items():
         setattr(p, k, v)

@@ -11,10 +11,47 @@
 
 namespace rh {
 
+// Voltage a clamp protocol sets after the step that starts at time t
+// (cuda_Cell_Detailed.cu:733-773); `v` is the voltage the membrane model
+// computed, returned unchanged by the paced protocols.
+__host__ __device__ inline double protocol_voltage(const CellConst& c, double t, double dt,
+                                                   double v) {
+  switch (c.protocol) {
+    case RH_PROTO_VCLAMP:  // :733-739
+      return t > 100 ? c.clamp_mv : -86;
+    case RH_PROTO_BROWN_VCLAMP:  // :741-752
+      if (t < 4000) return -86;
+      if (t < 4200) return -10;
+      if (t < 6200) return 10;
+      if (t < 7200) return -30;
+      return -86;
+    case RH_PROTO_AP_CLAMP:  // :754-757, one PCL of samples repeated
+      return c.apv[((int)(t / dt + 0.1)) % c.napv];
+    case RH_PROTO_LINEAR_AP_CLAMP:  // :758-773
+      if (t < 100) return -86;
+      if (t < 101.865) return 68 * (t - 100) - 80;
+      if (t < 119.1) return -(t - 100) + 48;
+      if (t < 138.9) return 27 + 0.1 * (t - 100);
+      if (t < 364.43) return 43 - (t - 100) / 3.2;
+      if (t < 395.43) return -1.5 * (t - 100) + 357;
+      return -86;
+    default:
+      return v;
+  }
+}
+
+// Stimulus current of the step that starts at time t (:689-699): 80 uA/uF
+// in the first ms of each period (phase from fmod(t + PCL - 100, PCL)),
+// none for unpaced and permeabilised cells.
+__host__ __device__ inline double stimulus(const CellConst& c, double phase) {
+  if (c.perm || c.protocol == RH_PROTO_NOPACING) return 0.0;
+  return phase < 1.0 ? 80.0 : 0.0;
+}
+
 // Membrane model step.  Expression order follows the reference so that the
 // device result agrees with it to the last few ulps.
-__host__ __device__ inline void membrane_update(rh_membrane& m, double dt, double tperid,
-                                                double svikr) {
+__host__ __device__ inline void membrane_update(rh_membrane& m, double dt, const CellConst& c) {
+  const double tperid = c.pcl, svikr = c.svikr;
   const double t = m.t, v = m.v;
   const double xki = 140.0, xko = 5.40;  // :350-351
   const double csubt = m.csubt;
@@ -102,7 +139,7 @@ __host__ __device__ inline void membrane_update(rh_membrane& m, double dt, doubl
   double fnak = 1.00 / (1.0 + 0.1245 * exp(-0.1 * v * FRT) + 0.0365 * sigma * exp(-v * FRT));
   double xinak = 1. * 1.5000 * fnak * (1.0 / (1.0 + pow((12.00 / xnai), 1.00))) * xko / (xko + 1.50);
   // stimulus (:689-692)
-  double stim = (fmod(t + tperid - 100, tperid) < 1.0) ? 80.0 : 0.0;
+  double stim = stimulus(c, fmod(t + tperid - 100, tperid));
   // [Na]i and V (:701-738)
   double wcainv = 1.0 / 50.0;
   double conv = 0.18 * 12500;
@@ -112,7 +149,7 @@ __host__ __device__ inline void membrane_update(rh_membrane& m, double dt, doubl
   double dvh = -(xina + xik1 + 1 * xikr + 1 * xiks + xitos + 1 * xitof + 1. * m.xinacato +
                  1 * m.xicatto + xinak) +
                stim;
-  m.v = v + dvh * dt;
+  m.v = protocol_voltage(c, t, dt, v + dvh * dt);
   m.out_ica += m.xicatto;  // :774-776
   m.out_ncx += m.xinacato;
   m.out_ina += xina;
@@ -180,6 +217,7 @@ __host__ __device__ inline bool step_coef(StepCoef<double>& k, const rh_membrane
   k.rdth95 = 0.95 / (dt / 5.0);
   k.reset_window = fmod(t - dt, OUTT) < dt;
   k.output_step = fmod(t + 0.0000001, OUTT) < dt;
+  k.perm = c.perm;
   k.cadist_step = k.output_step && fmod(t + 0.0000001, 5.0) < dt &&
                   fmod(t + 0.0000001, c.pcl) < 500.0;  // :1002
   return t < c.tend;

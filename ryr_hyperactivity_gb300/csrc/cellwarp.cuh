@@ -142,9 +142,10 @@ struct WarpSlots {
 // function also computes the three fmods of this step (stimulus phase and the
 // next lattice update's window flags: reset, output, and the two cadist
 // conditions) into fm[0..4].
-__device__ inline void membrane_update_warp(rh_membrane& m, double dt, double tperid,
-                                            double svikr, const double tot[3], int nin,
-                                            double* s, double fm[5]) {
+__device__ inline void membrane_update_warp(rh_membrane& m, double dt, const CellConst& c,
+                                            const double tot[3], double* s, double fm[5]) {
+  const double tperid = c.pcl, svikr = c.svikr;
+  const int nin = c.n;
   const int lane = threadIdx.x & 31;
   WarpSlots w{s, s + 32, s + 64, lane};
   const double t = m.t, v = m.v;
@@ -330,7 +331,7 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, double tp
   const double xitof = 1.0 * 0.10 * m.xtof * m.ytof * (v - ek);
   m.xtof = xtos_inf - (xtos_inf - m.xtof) * G[7];
   m.ytof = ytos_inf - (ytos_inf - m.ytof) * G[8];
-  const double stim = (fm[0] < 1.0) ? 80.0 : 0.0;
+  const double stim = stimulus(c, fm[0]);
   const double wcainv = 1.0 / 50.0;
   const double conv = 0.18 * 12500;
   const double xrr = 1.0 * (1.0 / wcainv / conv) / 1000.0;
@@ -339,7 +340,7 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, double tp
   const double dvh = -(xina + xik1 + 1 * xikr + 1 * xiks + xitos + 1 * xitof + 1. * m.xinacato +
                        1 * m.xicatto + xinak) +
                      stim;
-  m.v = v + dvh * dt;
+  m.v = protocol_voltage(c, t, dt, v + dvh * dt);
   m.out_ica += m.xicatto;
   m.out_ncx += m.xinacato;
   m.out_ina += xina;
@@ -457,6 +458,7 @@ __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
   k.dt = dt;
   k.reset_window = fm1 < dt;
   k.output_step = fm2 < dt;
+  k.perm = c.perm;
   k.cadist_step = k.output_step && fm[2] < dt && fm[3] < 500;
   return t < c.tend;
 }

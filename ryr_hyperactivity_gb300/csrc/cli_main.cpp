@@ -15,6 +15,11 @@
 //   --nx N --ny N --nz N --nbeats N --pcl MS   lattice and protocol
 //   --lqt 0|1 --iso2 0|1 --tapsi 0|1           build modes (Makefile:8-28)
 //   --cadist                                   outputcadist build (:1001-1013)
+//   --protocol paced|nopacing|vclamp|brownvclamp|apclamp|linearapclamp
+//                                              voltage protocol build (:34, :54-61);
+//                                              vclamp holds a3 mV after 100 ms,
+//                                              apclamp reads v_1000.txt (:383-395)
+//   --perm                                     permeabilised-cell build (:35)
 //   --mixed                                    FP32 lattice / FP64 whole-cell
 //   --seed S --ikr-scale X --cao MM --linescan-jz J --max-steps N
 #include <stdio.h>
@@ -30,7 +35,7 @@
 static void usage() {
   fprintf(stderr,
           "usage: cuda_Cell_Detailed <device> <name> a3 a4 a5 a6 a7 a8 a9 a10 [--nx N] [--ny N] "
-          "[--nz N] [--nbeats N] [--pcl MS] [--lqt 0|1] [--iso2 0|1] [--tapsi 0|1] [--cadist] [--mixed] "
+          "[--nz N] [--nbeats N] [--pcl MS] [--lqt 0|1] [--iso2 0|1] [--tapsi 0|1] [--cadist] [--protocol P] [--perm] [--mixed] "
           "[--seed S] [--ikr-scale X] [--cao MM] [--linescan-jz J] [--max-steps N]\n");
 }
 
@@ -74,6 +79,20 @@ int main(int argc, char** argv) {
     else if (k == "--tapsi") p.tapsi = atoi(next());
     else if (k == "--mixed") o.precision = RH_MIXED;
     else if (k == "--cadist") o.record_cadist = 1;
+    else if (k == "--perm") p.perm = 1;
+    else if (k == "--protocol") {
+      const std::string v = next();
+      if (v == "paced") p.protocol = RH_PROTO_PACED;
+      else if (v == "nopacing") p.protocol = RH_PROTO_NOPACING;
+      else if (v == "vclamp") p.protocol = RH_PROTO_VCLAMP;
+      else if (v == "brownvclamp") p.protocol = RH_PROTO_BROWN_VCLAMP;
+      else if (v == "apclamp") p.protocol = RH_PROTO_AP_CLAMP;
+      else if (v == "linearapclamp") p.protocol = RH_PROTO_LINEAR_AP_CLAMP;
+      else {
+        usage();
+        return 2;
+      }
+    }
     else if (k == "--seed") p.seed = (uint32_t)strtoul(next(), nullptr, 10);
     else if (k == "--ikr-scale") p.ikr_scale = atof(next());
     else if (k == "--cao") p.cao_mM = atof(next());
@@ -101,6 +120,28 @@ int main(int argc, char** argv) {
     rh_last_error(nullptr, buf, sizeof buf);
     fprintf(stderr, "rh_create failed: %s\n", buf);
     return 1;
+  }
+  if (p.protocol == RH_PROTO_AP_CLAMP) {  // :383-395: one PCL of samples from v_1000.txt
+    const int numsteps = (int)(p.pcl_ms / o.dt_ms + 0.1);
+    std::vector<double> varray(numsteps);
+    FILE* fv = fopen("v_1000.txt", "r");
+    int got = 0;
+    if (fv) {
+      while (got < numsteps && fscanf(fv, "%lf", &varray[got]) == 1) ++got;
+      fclose(fv);
+    }
+    if (got < numsteps) {
+      fprintf(stderr, "v_1000.txt: %d of the %d voltages the AP clamp needs\n", got, numsteps);
+      rh_destroy(sim);
+      return 1;
+    }
+    if (rh_set_ap_clamp(sim, 0, varray.data(), numsteps) != RH_OK) {
+      char buf[512];
+      rh_last_error(sim, buf, sizeof buf);
+      fprintf(stderr, "%s\n", buf);
+      rh_destroy(sim);
+      return 1;
+    }
   }
   printf("Initialization Complete\n");
   fflush(stdout);

@@ -70,6 +70,11 @@ struct CellConst {
   long long ls_off;  // first linescan row of this cell in the ring
   long long cd_off;  // first double of this cell's cadist records (record_cadist)
   double svica, svncx, sviup_tot, svikr, cao, ku, ku2, kb, pcl, tend;
+  int perm;            // permeabilised cell (rh_cell_params.perm)
+  int protocol;        // RH_PROTO_*
+  double clamp_mv;     // RH_PROTO_VCLAMP holding voltage
+  const double* apv;   // RH_PROTO_AP_CLAMP waveform (device), napv samples
+  int napv;
 };
 
 // Mutable per-cell state, owned by the device between host calls.

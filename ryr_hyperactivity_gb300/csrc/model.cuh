@@ -38,6 +38,10 @@ constexpr double TAUST = 1.42;
 constexpr double FRT = (96.485 / 8.314 / 308.0);
 constexpr double XI = 0.7;
 constexpr double CI_BASAL = 0.0944;
+// permeabilised cell (-Dperm, :87-89): basal [Ca]i held at the lattice faces
+// and in the submembrane leak; initial JSR/NSR load
+constexpr double PERM_CI_BASAL = 0.3;
+constexpr double PERM_CJSR_BASAL = 900;
 constexpr double VS = 0.025;
 constexpr double ICAGAMMA = 0.5;
 constexpr double CM = 45;
@@ -235,6 +239,7 @@ struct StepCoef {
   int reset_window;  // fmod(t-dt, outt) < dt (cuda_Cell_Detailed.cu:1244)
   int output_step;   // fmod(t+1e-7, outt) < dt (:777)
   int cadist_step;   // output step that also writes a cadist record (:1002)
+  int perm;          // permeabilised cell: no LCC/NCX, [Ca] faces held (-Dperm)
 };
 
 template <class R, class Q>
@@ -248,6 +253,7 @@ __host__ __device__ inline void convert_coef(StepCoef<R>& d, const StepCoef<Q>& 
   d.reset_window = s.reset_window;
   d.output_step = s.output_step;
   d.cadist_step = s.cadist_step;
+  d.perm = s.perm;
 }
 
 // ---- RyR transition draw (subroutine_cuda.c:332-363 and siblings) ----

@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <memory>
 #include <string>
@@ -61,6 +62,7 @@ struct rh_sim {
   double* d_out_ls = nullptr;
   double* d_out_cd = nullptr;  // cadist records (record_cadist), per cell from cd_off
   double* d_diag = nullptr;
+  std::vector<double*> d_apv;  // AP-clamp waveforms, per cell (rh_set_ap_clamp)
   rh_beat_stats* d_stats = nullptr;
   int64_t ls_rows_total = 0;
   // host mirror of each cell's clock (same IEEE additions as the device)
@@ -110,8 +112,9 @@ double csqn_bound_ss(double cjsr) {  // subroutine_cuda.c:179-195
 
 InitValues init_values(const rh_cell_params& p) {  // cuda_Cell_Detailed.cu:1108-1174
   InitValues v{};
-  double cjsr_b = p.tapsi ? 10 : p.cjsr_basal;
-  const double cb = CI_BASAL;
+  // :87-92 (perm fixes both basal values), :1118-1120 (tapsi overrides the load)
+  double cjsr_b = p.tapsi ? 10 : (p.perm ? PERM_CJSR_BASAL : p.cjsr_basal);
+  const double cb = p.perm ? PERM_CI_BASAL : CI_BASAL;
   v.cp = cb;
   v.cs = cb;
   v.cjsr = cjsr_b;
@@ -358,6 +361,8 @@ void rh_default_cell_params(rh_cell_params* p) {
   p->seed = 18;
   p->cell_id = 0;
   p->linescan_jz = -1;
+  p->protocol = RH_PROTO_PACED;
+  p->perm = 0;
 }
 
 void rh_default_run_opts(rh_run_opts* o) {
@@ -456,6 +461,15 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     cc.kb = p.kb;
     cc.pcl = p.pcl_ms;
     cc.tend = p.nbeats * p.pcl_ms + 2100;
+    if (p.protocol < RH_PROTO_PACED || p.protocol > RH_PROTO_LINEAR_AP_CLAMP)
+      return fail(s, RH_ERR_ARG, "cell %d: unknown protocol %d", c, p.protocol);
+    cc.perm = p.perm ? 1 : 0;
+    cc.protocol = p.protocol;
+    cc.clamp_mv = p.clamp_mv;
+    cc.apv = nullptr;  // rh_set_ap_clamp
+    cc.napv = p.protocol == RH_PROTO_AP_CLAMP ? (int)(p.pcl_ms / s->opts.dt_ms + 0.1) : 0;
+    if (p.protocol == RH_PROTO_AP_CLAMP && cc.napv < 1)
+      return fail(s, RH_ERR_ARG, "cell %d: AP clamp needs pcl_ms >= dt", c);
     off += (n64 + 31) & ~int64_t(31);
     ls_off += (int64_t)s->opts.output_capacity * cc.lx;
     if (s->opts.record_cadist)
@@ -603,6 +617,7 @@ int rh_destroy(rh_sim* s) {
   cudaFree(s->d_out_wc);
   cudaFree(s->d_out_ls);
   cudaFree(s->d_out_cd);
+  for (double* w : s->d_apv) cudaFree(w);
   cudaFree(s->d_diag);
   cudaFree(s->d_stats);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -619,6 +634,9 @@ int rh_destroy(rh_sim* s) {
 int rh_run_steps(rh_sim* s, int64_t nsteps) {
   if (!s || nsteps < 0) return RH_ERR_ARG;
   if (!s->stream) return fail(s, RH_ERR_STATE, "simulator not initialised");
+  for (int c = 0; c < s->ncells; ++c)
+    if (s->active_host[c] && s->hcells[c].protocol == RH_PROTO_AP_CLAMP && !s->hcells[c].apv)
+      return fail(s, RH_ERR_STATE, "cell %d: AP-clamp waveform not set (rh_set_ap_clamp)", c);
   CK(cudaSetDevice(s->device));
   if (s->opts.keep_diagnostics) {
     int r = ensure_diag(s);
@@ -689,6 +707,33 @@ int rh_lattice_step(rh_sim* s) {
   if (r) return r;
   CK(launch_one(s, false, true));
   CK(cudaStreamSynchronize(s->stream));
+  return RH_OK;
+}
+
+int rh_set_ap_clamp(rh_sim* s, int32_t cell, const double* v, int64_t n) {
+  int r = check_cell(s, cell);
+  if (r) return r;
+  const CellConst& cc = s->hcells[cell];
+  if (cc.protocol != RH_PROTO_AP_CLAMP)
+    return fail(s, RH_ERR_ARG, "cell %d: protocol is not RH_PROTO_AP_CLAMP", cell);
+  if (!v || n != cc.napv)
+    return fail(s, RH_ERR_ARG, "cell %d: AP-clamp waveform needs %d samples (pcl/dt), got %lld",
+                cell, cc.napv, (long long)n);
+  for (int64_t k = 0; k < n; ++k)
+    if (!std::isfinite(v[k])) return fail(s, RH_ERR_ARG, "cell %d: sample %lld is not finite",
+                                          cell, (long long)k);
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  if (s->d_apv.empty()) s->d_apv.assign(s->ncells, nullptr);
+  if (!s->d_apv[cell]) CK(cudaMalloc(&s->d_apv[cell], sizeof(double) * (size_t)n));
+  CK(cudaMemcpy(s->d_apv[cell], v, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice));
+  // every tile layout's copy of the cell constants points at the waveform
+  for (int k = 0; k < kNumTileSizes; ++k) {
+    rh_sim::TileSet& t = s->sets[k];
+    t.hcells[cell].apv = s->d_apv[cell];
+    CK(cudaMemcpy(t.d_cells + cell, &t.hcells[cell], sizeof(CellConst), cudaMemcpyHostToDevice));
+  }
+  s->hcells[cell].apv = s->d_apv[cell];
   return RH_OK;
 }
 

@@ -83,7 +83,7 @@ __noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool ou
   const double dt = a.dt;
   // reduction (:447-456) and membrane model (:458-739), warp-parallel
   double fm[5];
-  membrane_update_warp(m, dt, cc.pcl, cc.svikr, tot, cc.n, scratch, fm);
+  membrane_update_warp(m, dt, cc, tot, scratch, fm);
   uint32_t status = dyn->status;
   if (!isfinite(m.v) || !isfinite(m.xnai) || !isfinite(m.csubt) || !isfinite(m.xicatto) ||
       !isfinite(m.xinacato))
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       bfca = Math<R>::div(R(0.175), R(1) + qq * qq);
     }
     int nlcp = 0;
-    {
+    if (!k.perm) {  // a permeabilised cell has no LCC current (:1249-1263 under -Dperm)
       uint64_t slots = ((uint64_t)lccw.y << 32) | lccw.x;
 #pragma unroll 1
       for (int ll = 0; ll < 8; ++ll) {
@@ -446,8 +446,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       lccw.x = (uint32_t)slots;
       lccw.y = (uint32_t)(slots >> 32);
     }
-    R icat1;
-    {
+    R icat1 = R(0);
+    if (!k.perm) {
       R ica = k.lcc_k * (cpx * k.lcc_e2z_k - k.cao);
       if (ica > R(0)) ica = R(0);
       icat1 = k.svica * R(nlcp) * ica;
@@ -463,9 +463,10 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     R xire = R(0.0147 * SVJMAX) * po * (cjsr - cp) * R(1.0 / VP);
     if (xire < R(0)) xire = R(0);
 
-    // ---- NCX (:1296, subroutine_cuda.c:47-75) ----
-    R xinaca;
-    {
+    // ---- NCX (:1296, subroutine_cuda.c:47-75); none in a permeabilised cell,
+    //      whose xinaca keeps its initial 0 and Ancx its value (:1294-1300) ----
+    R xinaca = R(0);
+    if (!k.perm) {
       const R csm = cs0 * R(1e-3);
       const R t2 = R(KMNAO * KMNAO * KMNAO) * csm * (R(1) + csm * R(1.0 / KMCAI));
       const R t3 = k.ncx_t3a + csm * R(XNAO * XNAO * XNAO);
@@ -488,7 +489,10 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     R csn = cs0;
     {
       const R dth = k.dth, rdth95 = k.rdth95;
-      R csN = cs0, csS = cs0;
+      // z faces: zero flux (the ghost repeats cs), or the permeabilised
+      // cell's bath value, which its ghosts keep (:1603-1689 under -Dperm)
+      const R cs_face = k.perm ? R(PERM_CI_BASAL) : cs0;
+      R csN = cs_face, csS = cs_face;
       if (has_zp) csN = kStage ? s_hcs[1][tid] : __ldg(cs + g + lxly);
       if (has_zm) csS = kStage ? s_hcs[0][tid] : __ldg(cs + g - lxly);
       const R csdiff = (csN + csS - R(2) * cs0) * R(1.0 / TAUST);
@@ -502,7 +506,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         const R r_sar = buffer_rate<R>(R(KSARON), R(KSAROFF), R(BSAR), casar, csn, dth, rdth95);
         const R r_sarh =
             buffer_rate<R>(R(KSARHON), R(KSARHOFF), R(BSARH), casarh, csn, dth, rdth95);
-        const R dotcs = R(VP / VS / TAUPS) * (cp - csn) + cs_const - (r_sar + r_sarh);
+        R dotcs = R(VP / VS / TAUPS) * (cp - csn) + cs_const - (r_sar + r_sarh);
+        if (k.perm) dotcs += (R(PERM_CI_BASAL) - csn) * R(0.2);  // :1409-1411
         const R cpbuff = buffer_rate<R>(R(KSARON), R(KSAROFF), R(BSAR), casarj, cp, dth, rdth95);
         const R cpbuffh =
             buffer_rate<R>(R(KSARHON), R(KSARHOFF), R(BSARH), casarhj, cp, dth, rdth95);
@@ -550,7 +555,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     // adjacent CRUs' pair p.  Along y (x) the neighbour pair is p^1 (p^2) of
     // this CRU or of the adjacent CRU in the direction of the pair's y (x)
     // bit.  At a lattice face the zero-flux ghost equals the sub-voxel
-    // itself (:1601-1652), so that difference vanishes.
+    // itself (:1601-1652), so that difference vanishes; a permeabilised
+    // cell's ci ghosts instead keep the bath value (:1653-1689).
     const bool has_yp = y + 1 < ly, has_ym = y > 0;
     const bool has_xp = x + 1 < lx, has_xm = x > 0;
     const bool zp_in = tid + lxly < count, zm_in = tid - lxly >= 0;
@@ -588,6 +594,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         nb0 = catf2[gq], nb1 = cats2[gq], nb2 = cacal2[gq], nb3 = casr2[gq], nb4 = camyo2[gq];
         nb5 = mgmyo2[gq];
       }
+      // ci a face ghost holds: the sub-voxel's own value, or the bath
+      const V cface = k.perm ? splat2(R(PERM_CI_BASAL)) : c;
       // z
       V czp = c, nzp = n, czm = c, nzm = n;
       if (kStage) {
@@ -619,14 +627,14 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         }
       }
       }
-      const V ciN = v2(c.y, has_zp ? czp.x : c.y), cnN = v2(n.y, has_zp ? nzp.x : n.y);
-      const V ciS = v2(has_zm ? czm.y : c.x, c.x), cnS = v2(has_zm ? nzm.y : n.x, n.x);
+      const V ciN = v2(c.y, has_zp ? czp.x : cface.y), cnN = v2(n.y, has_zp ? nzp.x : n.y);
+      const V ciS = v2(has_zm ? czm.y : cface.x, c.x), cnS = v2(has_zm ? nzm.y : n.x, n.x);
       // y: pair p^1
       V ciE, cnE, ciW, cnW;
       {
         const int py = p ^ 1;
         const V ci_in = s_ci2[py][tid], cn_in = s_cn2[py][tid];
-        V ci_ex = c, cn_ex = n;
+        V ci_ex = cface, cn_ex = n;
         const int d = by ? lx : -lx;
         if (by ? has_yp : has_ym) {
           if (kStage) {
@@ -650,7 +658,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       {
         const int px = p ^ 2;
         const V ci_in = s_ci2[px][tid], cn_in = s_cn2[px][tid];
-        V ci_ex = c, cn_ex = n;
+        V ci_ex = cface, cn_ex = n;
         const int d = bx ? 1 : -1;
         if (bx ? has_xp : has_xm) {
           if (bx ? xp_in : xm_in) {

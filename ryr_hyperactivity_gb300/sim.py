@@ -87,6 +87,13 @@ class Simulator:
     def lattice_step(self) -> None:
         self._ck(self.L.rh_lattice_step(self.h))
 
+    def set_ap_clamp(self, cell: int, v_mV) -> None:
+        """Waveform of an AP-clamp cell (protocol "apclamp"): one voltage per
+        step of one PCL, (int)(pcl/dt + 0.1) samples."""
+        a = np.ascontiguousarray(v_mV, np.float64)
+        self._ck(self.L.rh_set_ap_clamp(self.h, cell, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                        len(a)))
+
     # -- state
     def get_state(self, cell: int = 0) -> HostState:
         hs = HostState(self.n[cell])

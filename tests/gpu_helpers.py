@@ -84,3 +84,28 @@ def field_errors(got: HostState, ref: HostState, mask=None, fields=None):
             g, r = g[mask], r[mask]
         out[f] = rel_err(g, r)
     return out
+
+
+def ap_waveform(pcl_ms: float, dt: float = 0.025) -> np.ndarray:
+    """Synthetic action-potential clamp waveform, one sample per step of one
+    PCL ((int)(pcl/dt + 0.1) samples, the length the reference reads from
+    v_1000.txt, cuda_Cell_Detailed.cu:383-395): rest at -86 mV, a 2 ms
+    upstroke to +40 mV at 10 ms, then a quadratic repolarisation over 140 ms.
+    Values are rounded to 1e-6 mV so that their decimal text parses back to
+    the same doubles."""
+    n = int(pcl_ms / dt + 0.1)
+    t = np.arange(n) * dt
+    v = np.full(n, -86.0)
+    up = (t >= 10) & (t < 12)
+    v[up] = -86 + (t[up] - 10) / 2 * 126
+    pl = t >= 12
+    v[pl] = 40 - 126 * np.clip((t[pl] - 12) / 140, 0, 1) ** 2
+    return np.round(v, 6)
+
+
+def variant_params(spec: dict):
+    """Cell parameters of a recorded reference run (tests/golden/ref_full_runs.json)."""
+    from ryr_hyperactivity_gb300.abi import cell_params
+    a = spec["args"]
+    return cell_params(clamp_mv=a[0], cjsr_basal=a[1], ncx_scale=a[2], ku=a[3], r1=a[4], kb=a[5],
+                       ica_scale=a[6], ku2=a[7], seed=spec["seed"], **spec["cell"])

@@ -54,6 +54,37 @@ def test_oracle_cadist_matches_reference():
     assert hashlib.sha256(text.encode()).hexdigest() == spec["cadist_sha256"]
 
 
+# wholecell columns of the window accumulators out_ncx, out_ica, out_ina
+# (:1044-1045, :1058): the reference leaves them uninitialised before the first
+# output window (:332-334), the oracle starts them at 0
+WINDOW_COLS = (3, 4, 17)
+PROTOCOL_VARIANTS = ["vclamp", "brownvclamp", "apclamp", "linearapclamp", "nopacing", "perm"]
+
+
+@pytest.mark.parametrize("variant", PROTOCOL_VARIANTS)
+def test_oracle_matches_reference_protocol_build(variant):
+    """The voltage protocols and the permeabilised cell against the reference
+    built with the matching switch: every wholetest_ and linescan_ byte,
+    except the first record's uninitialised window accumulators."""
+    from tests.gpu_helpers import ap_waveform, variant_params
+    spec = META[variant]
+    p = variant_params(spec)
+    o = O.Oracle(p)
+    if variant == "apclamp":
+        o.set_ap_clamp(ap_waveform(p.pcl_ms))
+    _, wc, ls = o.run(spec["steps"], max_rec=spec["wholetest_lines"] + 1)
+    wt = O.wholecell_text(wc)
+    assert len(wc) == spec["wholetest_lines"]
+    first, rest = wt.split("\n", 1)
+    got, want = first.split(), spec["wholetest_first_line"].split()
+    assert len(got) == len(want) == 45
+    assert [g for k, g in enumerate(got) if k not in WINDOW_COLS] == \
+        [w for k, w in enumerate(want) if k not in WINDOW_COLS]
+    assert hashlib.sha256(rest.encode()).hexdigest() == spec["wholetest_rest_sha256"]
+    lst = O.linescan_text(ls)
+    assert hashlib.sha256(lst.encode()).hexdigest() == spec["linescan_sha256"]
+
+
 @pytest.mark.slow
 def test_oracle_matches_reference_full_run():
     p, spec = _params("c1")
