@@ -82,6 +82,12 @@ extern "C" {
                                       given with rh_set_ap_clamp */
 #define RH_PROTO_LINEAR_AP_CLAMP 5 /* -Dlinearapclamp: piecewise-linear AP (:758-773) */
 
+/* Sarcolemmal Na/Ca exchanger forms (subroutine_cuda.c:47-120). */
+#define RH_NCX_ALLOSTERIC 0  /* ncx: Ka = Ancx with its own ODE (the reference's build) */
+#define RH_NCX_OLD 1         /* oldncx: Ka = 1/(1+(Kda/cs)^3), Ancx from on/off rates
+                                (the commented call at cuda_Cell_Detailed.cu:1300) */
+#define RH_NCX_NOALLO 2      /* ncx_noallo: no allosteric state, Ka = 1 above -75 mV */
+
 /* Parameters of one cell.  argv[k] refers to the reference command line
  * (cuda_Cell_Detailed <dev> <name> a3 .. a10). */
 typedef struct {
@@ -111,6 +117,16 @@ typedef struct {
                            stimulus, [Ca] 0.3 uM held at the lattice faces and
                            leaking into the submembrane space (:1409-1411), initial
                            [Ca]i 0.3 uM and JSR 900 uM (argv[4] unused, :87-93) */
+  int32_t iso;          /* -Diso (:32): isoproterenol from t = 5.5 PCL: SERCA x2
+                           (x1.75 still wins under iso2), LCC slots 4-7 filled at
+                           t = 5.5 PCL (+15.5 PCL ...), stimulus at phase 0 and
+                           only while t < 11.9 PCL (:683-687, :1213-1229) */
+  int32_t randomlcc;    /* -Drandomlcc (:31): each CRU starts with 0..8 LCCs, one
+                           Philox draw per CRU at initialisation (:1150-1155) */
+  int32_t slowncx;      /* -Dslowncxchange (:52): background Ca current in the
+                           submembrane space, NCX Ka = 5 Ancx, slower IKs Ca
+                           dependence (:540-543, :1267-1269, subroutine_cuda.c:59-62) */
+  int32_t ncx_form;     /* RH_NCX_* (default RH_NCX_ALLOSTERIC) */
 } rh_cell_params;
 
 /* Run-wide options. */

@@ -24,6 +24,10 @@
  *                                                of the same draw)
  *   uint32    = w[2h]                           (the reference's curand())
  * The (0,1] range is the one curand_uniform_double has.
+ *
+ * Draws made while the lattice is initialised (the LCC count of a randomlcc
+ * cell, cuda_Cell_Detailed.cu:1150-1151) use step = RH_PHILOX_INIT_STEP, a
+ * value no lattice update reaches.
  */
 #ifndef RH_PHILOX_H
 #define RH_PHILOX_H
@@ -35,6 +39,8 @@
 #else
 #define RH_HD static inline
 #endif
+
+#define RH_PHILOX_INIT_STEP 0xFFFFFFFFFFFFFFFFull
 
 #define RH_PHILOX_M0 0xD2511F53u
 #define RH_PHILOX_M1 0xCD9E8D57u

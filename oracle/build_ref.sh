@@ -13,10 +13,18 @@
 #       - the <<<grid,block>>> launches turned into REF_LAUNCH(...) calls of the
 #         host shim (oracle/ref_shim/ref_shim.h), Compute counted as one step;
 #       - the linescan plane (hard-coded jz = 5) and the RNG seed (18) made
-#         overridable, and the time loop bounded by REF_MAX_STEPS when set.
+#         overridable, and the time loop bounded by REF_MAX_STEPS when set;
+#       - the NCX call of Compute (:1296) routed through REF_NCX, so that a
+#         variant can select the reference's oldncx or ncx_noallo instead.
 #   oracle/_ref/gen/*.c, reesica.h   the three device files it includes, copied
 #       so that the generated program builds where the reference is absent.
 #   oracle/_ref/ref_<variant>         host executables (g++ -fopenmp).
+# The LCC loop of Compute tests lcc[ll] < 16 before ll < 8 (:1253), so a CRU
+# with all eight slots filled (iso after 5.5 PCL, randomlcc) reads lcc[8], one
+# int past the array.  g++ -O2 takes that read as proof that ll < 8 always
+# holds, drops the bound and runs the loop on through nl, nou, ncu ...;
+# -fno-aggressive-loop-optimizations keeps the bound, so the loop stops after
+# slot 8 as written.
 # Usage: build_ref.sh [variant ...]   (default: all variants below)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
@@ -35,6 +43,7 @@ if [ -f "$REF_SRC/cuda_Cell_Detailed.cu" ]; then
       -e 's/Compute<<<numBlocks, threadsPerBlock>>>\((.*)\);/REF_LAUNCH_STEP(Compute(\1));/' \
       -e 's/int jz = 5;/int jz = REF_LINESCAN_JZ;/' \
       -e 's/while \(t<nbeat\*tperid\+2100\)\{/while (t<nbeat*tperid+2100 \&\& ref_continue()){/' \
+      -e 's/CRU\[ac\]\.xinaca=sv_ncx\*svncx_lqt\*ncx\(/CRU[ac].xinaca=sv_ncx*svncx_lqt*REF_NCX(/' \
       > "$GEN/ref_fixA.cpp.tmp"
   for f in subroutine_cuda.c reesica.h buffers.c; do cp "$REF_SRC/$f" "$GEN/$f"; done
   mv "$GEN/ref_fixA.cpp.tmp" "$GEN/ref_fixA.cpp"
@@ -43,7 +52,7 @@ elif [ ! -f "$GEN/ref_fixA.cpp" ]; then
   exit 3
 fi
 
-for pat in 'REF_LAUNCH_STEP(Compute' 'REF_LAUNCH(Init' 'REF_LAUNCH(setup_kernel' 'REF_LINESCAN_JZ' 'ref_continue'; do
+for pat in 'REF_LAUNCH_STEP(Compute' 'REF_LAUNCH(Init' 'REF_LAUNCH(setup_kernel' 'REF_LINESCAN_JZ' 'ref_continue' 'svncx_lqt\*REF_NCX('; do
   grep -q "$pat" "$GEN/ref_fixA.cpp" || { echo "build_ref.sh: patch '$pat' did not apply" >&2; exit 4; }
 done
 
@@ -67,6 +76,13 @@ declare -A VARIANTS=(
   [linearapclamp]="-Dnx=12 -Dny=8 -Dnz=5 -Dnbeat=1 -Dtperid=1000.0 -DREF_LINESCAN_JZ=2 -Dlinearapclamp"
   [nopacing]="-Dnx=12 -Dny=8 -Dnz=5 -Dnbeat=1 -Dtperid=400.0 -DREF_LINESCAN_JZ=2 -Diso2 -Dlqt -Dnopacing"
   [perm]="-Dnx=12 -Dny=9 -Dnz=6 -Dnbeat=1 -Dtperid=1000.0 -DREF_LINESCAN_JZ=3 -Dperm"
+  # the rarer builds: time-dependent isoproterenol (alone and with make il),
+  # slowncxchange, and the two NCX functions no build calls
+  [iso]="-Dnx=8 -Dny=6 -Dnz=5 -Dnbeat=13 -Dtperid=100.0 -DREF_LINESCAN_JZ=2 -Diso"
+  [iso_il]="-Dnx=8 -Dny=6 -Dnz=5 -Dnbeat=13 -Dtperid=100.0 -DREF_LINESCAN_JZ=2 -Diso -Diso2 -Dlqt"
+  [slowncxchange]="-Dnx=12 -Dny=8 -Dnz=5 -Dnbeat=1 -Dtperid=400.0 -DREF_LINESCAN_JZ=2 -Dslowncxchange"
+  [oldncx]="-Dnx=12 -Dny=8 -Dnz=5 -Dnbeat=1 -Dtperid=400.0 -DREF_LINESCAN_JZ=2 -DREF_NCX_OLD"
+  [ncx_noallo]="-Dnx=12 -Dny=8 -Dnz=5 -Dnbeat=1 -Dtperid=400.0 -DREF_LINESCAN_JZ=2 -DREF_NCX_NOALLO"
 )
 want=("$@")
 if [ ${#want[@]} -eq 0 ]; then want=("${!VARIANTS[@]}"); fi
@@ -74,7 +90,7 @@ pids=()
 for v in "${want[@]}"; do
   defs="${VARIANTS[$v]:?unknown variant $v}"
   # shellcheck disable=SC2086
-  $CXX -std=c++17 -O2 -fopenmp -ffp-contract=off -w -x c++ \
+  $CXX -std=c++17 -O2 -fno-aggressive-loop-optimizations -fopenmp -ffp-contract=off -w -x c++ \
     -include "$HERE/ref_shim/ref_shim.h" -I "$HERE/ref_shim/include" -I "$GEN" \
     -DREF_SEED=18 $defs "$GEN/ref_fixA.cpp" -o "$OUT/ref_$v" -lm &
   pids+=($!)

@@ -122,6 +122,18 @@ inline bool ref_continue() {
   return (long long)g_ref_step < g_ref_max_steps;
 }
 
+/* The NCX call of Compute (cuda_Cell_Detailed.cu:1296), rewritten by
+ * build_ref.sh to REF_NCX(...): the reference's ncx, or with REF_NCX_OLD the
+ * oldncx of its commented alternative call (:1300), or with REF_NCX_NOALLO
+ * its ncx_noallo (subroutine_cuda.c:102), which takes no allosteric state. */
+#if defined(REF_NCX_NOALLO)
+#define REF_NCX(cs, v, tp, na, ancx, dt) ncx_noallo(cs, v, tp, na)
+#elif defined(REF_NCX_OLD)
+#define REF_NCX oldncx
+#else
+#define REF_NCX ncx
+#endif
+
 /* nx, ny, nz are the reference's lattice macros, visible where these expand. */
 #define REF_LAUNCH(...) ref_launch_all(nx, ny, nz, [&]() { __VA_ARGS__; })
 #define REF_LAUNCH_STEP(...)                                \

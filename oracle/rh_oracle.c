@@ -69,6 +69,7 @@
 #define KMCAO 1.3
 #define KMNAI 12.3
 #define KMNAO 87.5
+#define KDA 0.0003
 #define KSAT 0.27
 #define ETA 0.35
 #define FARAD 96.485
@@ -138,6 +139,8 @@ struct orc_sim {
   double dt;
   /* run constants derived from the parameters */
   double svica, svncx, sviup_tot, svikr, cao, tend;
+  double sviup_iso; /* SERCA prefactor once iso is active (t >= 5.5 PCL) */
+  double sviup_now; /* the prefactor of the lattice update in progress */
   int jz_line;
   /* per CRU */
   double *cp, *cjsr, *cjsrb, *ancx, *xire, *po, *xinaca, *xicat;
@@ -188,10 +191,13 @@ static inline double myo_mg_rate(double camyo, double mgmyo, double dt) {
 
 /* --------------------------- subroutine_cuda.c --------------------------- */
 
-/* Allosteric NCX with its activation state (subroutine_cuda.c:47-75). */
-static double ncx_flux(double cs, double v, double xnai, double* ancx, double dt, double cext) {
+/* Allosteric NCX with its activation state (subroutine_cuda.c:47-75); the
+ * slowncxchange build scales Ka by 5 (:59-62). */
+static double ncx_flux(double cs, double v, double xnai, double* ancx, double dt, double cext,
+                       int slowncx) {
   double za = v * FARAD / XRGAS / TEMPER;
   double ka = *ancx;
+  if (slowncx) ka = *ancx * 5;
   double t1 = KMCAI * CUBE(XNAO) * (1.0 + CUBE(xnai / KMNAI));
   double t2 = CUBE(KMNAO) * cs * (1.0 + cs / KMCAI);
   double t3 = (KMCAO + cext) * CUBE(xnai) + cs * CUBE(XNAO);
@@ -201,6 +207,39 @@ static double ncx_flux(double cs, double v, double xnai, double* ancx, double dt
   double ancxdot = (1.0 / (1.0 + CUBE(0.0003 / cs)) - *ancx) / 150.;
   *ancx += ancxdot * dt;
   return inaca;
+}
+
+/* NCX with the Ca-dependent Ka and the Mahajan t2, and the allosteric state
+ * from on/off rates (oldncx, subroutine_cuda.c:77-100). */
+static double ncx_old_flux(double cs, double v, double xnai, double* ancx, double dt,
+                           double cext) {
+  const double kncxoff = 0.00005;
+  const double kncxon = 2.53e-3 * 0.05;
+  double za = v * FARAD / XRGAS / TEMPER;
+  double ka = 1.0 / (1.0 + CUBE(KDA / cs));
+  double t1 = KMCAI * CUBE(XNAO) * (1.0 + CUBE(xnai / KMNAI));
+  double t2 = CUBE(KMNAO) * cs + CUBE(KMNAI) * cext * (1.0 + cs / KMCAI);
+  double t3 = (KMCAO + cext) * CUBE(xnai) + cs * CUBE(XNAO);
+  double inaca = ka * VNACA *
+                 (exp(ETA * za) * CUBE(xnai) * cext - exp((ETA - 1.0) * za) * CUBE(XNAO) * cs) /
+                 ((t1 + t2 + t3) * (1.0 + KSAT * exp((ETA - 1.0) * za)));
+  double ancxdot = (kncxon * SQ(cs * 1000) * (1 - *ancx) - *ancx * kncxoff);
+  if (kncxon * SQ(cs * 1000) * dt > 0.95) ancxdot = 0.95 / dt * (1 - *ancx) - *ancx * kncxoff;
+  *ancx += ancxdot * dt;
+  return inaca;
+}
+
+/* NCX without an allosteric state (ncx_noallo, subroutine_cuda.c:102-120). */
+static double ncx_noallo_flux(double cs, double v, double xnai, double cext) {
+  double za = v * FARAD / XRGAS / TEMPER;
+  double ka = 1.;
+  if (v < -75) ka = 1.0 / (1.0 + CUBE(KDA / cs));
+  double t1 = KMCAI * CUBE(XNAO) * (1.0 + CUBE(xnai / KMNAI));
+  double t2 = CUBE(KMNAO) * cs + CUBE(KMNAI) * cext * (1.0 + cs / KMCAI);
+  double t3 = (KMCAO + cext) * CUBE(xnai) + cs * CUBE(XNAO);
+  return ka * VNACA *
+         (exp(ETA * za) * CUBE(xnai) * cext - exp((ETA - 1.0) * za) * CUBE(XNAO) * cs) /
+         ((t1 + t2 + t3) * (1.0 + KSAT * exp((ETA - 1.0) * za)));
 }
 
 /* SERCA uptake (subroutine_cuda.c:128-137). */
@@ -510,7 +549,13 @@ static void init_lattice(orc_sim* s) {
     s->casarh[ac] = KSARHON * CI_B * BSARH / (KSARHON * CI_B + KSARHOFF);
     s->casarj[ac] = KSARON * CI_B * BSAR / (KSARON * CI_B + KSAROFF);
     s->casarhj[ac] = KSARHON * CI_B * BSARH / (KSARHON * CI_B + KSARHOFF);
-    for (int ll = 0; ll < 8; ++ll) s->lcc[ac * 8 + ll] = (ll < SVNCP) ? 3 : 16;
+    int randpoint = SVNCP; /* :1150-1155 */
+    if (s->p.randomlcc) {
+      rh_stream st;
+      rh_stream_init(&st, s->p.seed, s->p.cell_id, (uint32_t)ac, RH_PHILOX_INIT_STEP);
+      randpoint = (int)(rh_uniform_u32(&st) % 9u);
+    }
+    for (int ll = 0; ll < 8; ++ll) s->lcc[ac * 8 + ll] = (ll < randpoint) ? 3 : 16;
     double roo2 = RATEDIMER / (1.0 + pow(KDIMER / (cjsr_b), HILLDIMER));
     double aub = (-1.0 + sqrt(1.0 + 8.0 * CSQBERS * roo2)) / (4.0 * roo2 * CSQBERS) / TAUB;
     double abu = 1.0 / TAUU;
@@ -541,6 +586,10 @@ static void update_cru(orc_sim* s, int i, int j, int k, double v, double t, doub
   rh_stream rng;
   rh_stream_init(&rng, s->p.seed, s->p.cell_id, (uint32_t)ac, (uint64_t)s->m.step);
 
+  if (s->p.iso && fmod(t + 10 * s->p.pcl_ms, 15.5 * s->p.pcl_ms) < dt) { /* :1213-1218 */
+    for (int ll = 4; ll < 8; ++ll)
+      if (s->lcc[ac * 8 + ll] == 16) s->lcc[ac * 8 + ll] = 3;
+  }
   if (fmod(t - dt, OUTT) < dt) { /* window reset (:1244-1247) */
     s->nspark[ac] = 0;
     s->nl[ac] = 0;
@@ -562,7 +611,9 @@ static void update_cru(orc_sim* s, int i, int j, int k, double v, double t, doub
     }
     icat1 = s->svica * (double)(nlcp)*lcc_flux(v, cpx, s->cao);
   }
-  const double pmca = 0, bcgcur = 0; /* :1265-1269, both zero in the default build */
+  const double pmca = 0; /* :1265 */
+  double bcgcur = 0;
+  if (s->p.slowncx) bcgcur = 1.0 * 0.003016 / 32. * (v - log(180000 / cs[ac]) / 2. / FRT); /* :1268 */
   s->xicat[ac] = icat1 + pmca + bcgcur * (VS / VP);
 
   /* RyR gating and release (:1274-1293) */
@@ -574,15 +625,21 @@ static void update_cru(orc_sim* s, int i, int j, int k, double v, double t, doub
   s->xire[ac] = jsr_release(s->po[ac], s->cjsr[ac], s->cp[ac]) / randomi;
   if (s->xire[ac] < 0) s->xire[ac] = 0;
 
-  /* NCX (:1296); not computed in the perm build (:1294-1300), where
-   * xinaca keeps its zero-filled start and Ancx its initial value */
-  if (!s->p.perm)
-    s->xinaca[ac] = s->svncx * 1.0 * ncx_flux(cs[ac] / 1000.0, v, xnai, &s->ancx[ac], dt, s->cao);
+  /* NCX (:1296); zero in the perm build, Ancx then keeps its value (:1302) */
+  if (s->p.perm)
+    s->xinaca[ac] = 0;
+  else if (s->p.ncx_form == RH_NCX_OLD) /* the commented alternative call, :1300 */
+    s->xinaca[ac] = s->svncx * 1.0 * ncx_old_flux(cs[ac] / 1000.0, v, xnai, &s->ancx[ac], dt, s->cao);
+  else if (s->p.ncx_form == RH_NCX_NOALLO)
+    s->xinaca[ac] = s->svncx * 1.0 * ncx_noallo_flux(cs[ac] / 1000.0, v, xnai, s->cao);
+  else
+    s->xinaca[ac] = s->svncx * 1.0 *
+                    ncx_flux(cs[ac] / 1000.0, v, xnai, &s->ancx[ac], dt, s->cao, s->p.slowncx);
 
   /* SERCA and leak per sub-voxel (:1305-1308) */
   for (int ii = 0; ii < 8; ++ii) {
     int a8 = ac * 8 + ii;
-    s->xiup[a8] = s->sviup_tot * serca(ci[a8], cnsr[a8]);
+    s->xiup[a8] = s->sviup_now * serca(ci[a8], cnsr[a8]);
     s->xileak[a8] = SVILEAK * sr_leak(cnsr[a8], ci[a8]);
   }
   /* dyad / submembrane / JSR couplings (:1309-1317) */
@@ -756,6 +813,7 @@ static void apply_ghost_faces(orc_sim* s) {
 
 void orc_lattice_step(orc_sim* s) {
   const double v = s->m.v, t = s->m.t, xnai = s->m.xnai;
+  s->sviup_now = (s->p.iso && t >= 5.5 * s->p.pcl_ms) ? s->sviup_iso : s->sviup_tot; /* :1219 */
   const int lx = s->nx - 2, ly = s->ny - 2, lz = s->nz - 2;
   const int n = lx * ly * lz;
   uint32_t st = 0;
@@ -841,6 +899,10 @@ static void membrane_update(orc_sim* s) {
   double prnak = 0.0183300;
   double qks_inf = 0.2 * (1 + 0.8 / (1 + pow((0.28 / csubt), 3)));
   double tauqks = 1000.00;
+  if (s->p.slowncx) { /* :540-543 */
+    qks_inf = 0.2 * (1 + 1.6 / (1 + pow((0.28 / csubt), 3)));
+    tauqks = 2000;
+  }
   double eks = (1.00 / FRT) * log((xko + prnak * XNAO) / (xki + prnak * xnai));
   double xs1ss = 1.0 / (1.0 + exp(-(v - 1.500) / 16.700));
   double tauxs = 1.00 / (0.0000719 * (v + 30.00) / (1.00 - exp(-0.1480 * (v + 30.0))) +
@@ -892,9 +954,13 @@ static void membrane_update(orc_sim* s) {
   double fnak = 1.00 / (1.0 + 0.1245 * exp(-0.1 * v * FRT) + 0.0365 * sigma * exp(-v * FRT));
   double xinak =
       svnak * xibarnak * fnak * (1.0 / (1.0 + pow((xkmnai / xnai), hh))) * xko / (xko + xkmko);
-  /* stimulus (:689-692); none in the nopacing and perm builds (:694-699) */
+  /* stimulus (:689-692; iso :683-687); none in the nopacing and perm builds
+   * (:694-699) */
   double stim;
-  if (fmod(t + tperid - 100, tperid) < 1.0) stim = 80.0;
+  if (s->p.iso) {
+    if (fmod(t, tperid) < 1.0 && (t < tperid * 11.9)) stim = 80.0;
+    else stim = 0.0;
+  } else if (fmod(t + tperid - 100, tperid) < 1.0) stim = 80.0;
   else stim = 0.0;
   if (s->p.protocol == RH_PROTO_NOPACING || s->p.perm) stim = 0.0;
   /* [Na]i and V (:701-738) */
@@ -1260,6 +1326,12 @@ orc_sim* orc_create(const rh_cell_params* p, double dt) {
   if (p->tapsi) sviup = 0;
   double sviup_lqt = (p->lqt && p->tapsi) ? 0.05 : 0.; /* :121-125, :135 */
   s->sviup_tot = sviup + sviup_lqt;
+  /* the iso block sets sv_iup*2 from 5.5 PCL on, then iso2 and tapsi
+   * override it as before (:1219-1238) */
+  double sviup_iso = SV_IUP * 2.;
+  if (p->iso2) sviup_iso = SV_IUP * 1.75;
+  if (p->tapsi) sviup_iso = 0;
+  s->sviup_iso = sviup_iso + sviup_lqt;
   s->svikr = p->lqt ? 0 : 3 * p->ikr_scale; /* :128, :138 */
   s->cao = p->cao_mM;
   s->tend = p->nbeats * p->pcl_ms + 2100; /* :399 */

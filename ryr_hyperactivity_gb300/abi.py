@@ -27,10 +27,14 @@ RH_PROTO_VCLAMP = 2
 RH_PROTO_BROWN_VCLAMP = 3
 RH_PROTO_AP_CLAMP = 4
 RH_PROTO_LINEAR_AP_CLAMP = 5
+RH_NCX_ALLOSTERIC = 0
+RH_NCX_OLD = 1
+RH_NCX_NOALLO = 2
 # protocol names as the reference's build switches spell them
 PROTOCOLS = {"paced": RH_PROTO_PACED, "nopacing": RH_PROTO_NOPACING, "vclamp": RH_PROTO_VCLAMP,
              "brownvclamp": RH_PROTO_BROWN_VCLAMP, "apclamp": RH_PROTO_AP_CLAMP,
              "linearapclamp": RH_PROTO_LINEAR_AP_CLAMP}
+NCX_FORMS = {"ncx": RH_NCX_ALLOSTERIC, "oldncx": RH_NCX_OLD, "ncx_noallo": RH_NCX_NOALLO}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -57,6 +61,10 @@ class CellParams(C.Structure):
         ("linescan_jz", C.c_int32),
         ("protocol", C.c_int32),
         ("perm", C.c_int32),
+        ("iso", C.c_int32),
+        ("randomlcc", C.c_int32),
+        ("slowncx", C.c_int32),
+        ("ncx_form", C.c_int32),
     ]
 
 
@@ -129,10 +137,13 @@ def cell_params(**kw) -> CellParams:
     d = dict(nx=64, ny=28, nz=12, nbeats=7, pcl_ms=4000.0, clamp_mv=1.0, cjsr_basal=740.0,
              ncx_scale=1.0, ku=3.333, r1=0.0, kb=18.0, ica_scale=0.7, ku2=1.0, ikr_scale=1.0,
              cao_mM=1.8, lqt=1, iso2=1, tapsi=0, seed=18, cell_id=0, linescan_jz=-1,
-             protocol=RH_PROTO_PACED, perm=0)
+             protocol=RH_PROTO_PACED, perm=0, iso=0, randomlcc=0, slowncx=0,
+             ncx_form=RH_NCX_ALLOSTERIC)
     d.update(kw)
     if isinstance(d["protocol"], str):  # a build-switch name, e.g. "vclamp"
         d["protocol"] = PROTOCOLS[d["protocol"]]
+    if isinstance(d["ncx_form"], str):  # the reference's function name
+        d["ncx_form"] = NCX_FORMS[d["ncx_form"]]
     p = CellParams()
     for k, v in d.items():
         setattr(p, k, v)

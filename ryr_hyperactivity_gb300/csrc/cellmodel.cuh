@@ -40,12 +40,30 @@ __host__ __device__ inline double protocol_voltage(const CellConst& c, double t,
   }
 }
 
-// Stimulus current of the step that starts at time t (:689-699): 80 uA/uF
-// in the first ms of each period (phase from fmod(t + PCL - 100, PCL)),
-// none for unpaced and permeabilised cells.
-__host__ __device__ inline double stimulus(const CellConst& c, double phase) {
+// Stimulus current of the step that starts at time t (:683-699): 80 uA/uF
+// in the first ms of each period, none for unpaced and permeabilised cells.
+// `phase` is fmod(t + PCL - 100, PCL), or fmod(t, PCL) for an iso cell,
+// which is paced only while t < 11.9 PCL.
+__host__ __device__ inline double stimulus(const CellConst& c, double t, double phase) {
   if (c.perm || c.protocol == RH_PROTO_NOPACING) return 0.0;
+  if (c.iso) return (phase < 1.0 && t < c.pcl * 11.9) ? 80.0 : 0.0;
   return phase < 1.0 ? 80.0 : 0.0;
+}
+
+// Coefficients of the build options for the lattice update at time t with
+// voltage v: iso's SERCA boost and LCC insertion (:1213-1229; iso_phase =
+// fmod(t + 10 PCL, 15.5 PCL)), the NCX form, slowncxchange's background
+// current (:1267-1269).
+__host__ __device__ inline void option_coef(StepCoef<double>& k, const CellConst& c, double v,
+                                            double t, double dt, double iso_phase) {
+  k.sviup = (c.iso && t >= 5.5 * c.pcl) ? c.sviup_iso : c.sviup_tot;
+  k.iso_add_lcc = c.iso && iso_phase < dt;
+  k.ncx_form = c.ncx_form;
+  k.ncx_ka_hill = c.ncx_form == RH_NCX_OLD || (c.ncx_form == RH_NCX_NOALLO && v < -75);
+  k.ncx_t2b = (KMNAI * KMNAI * KMNAI) * c.cao;
+  k.slowncx = c.slowncx;
+  k.bcg_a = BCG_G * v;
+  k.bcg_b = BCG_G / 2. / FRT;
 }
 
 // Membrane model step.  Expression order follows the reference so that the
@@ -95,8 +113,8 @@ __host__ __device__ inline void membrane_update(rh_membrane& m, double dt, const
   m.xr = xkrinf - (xkrinf - m.xr) * exp(-dt / taukr);
   // IKs (:534-559)
   double prnak = 0.0183300;
-  double qks_inf = 0.2 * (1 + 0.8 / (1 + pow((0.28 / csubt), 3.0)));
-  double tauqks = 1000.00;
+  double qks_inf = 0.2 * (1 + (c.slowncx ? 1.6 : 0.8) / (1 + pow((0.28 / csubt), 3.0)));
+  double tauqks = c.slowncx ? 2000 : 1000.00;  // :540-543
   double eks = (1.00 / FRT) * log((xko + prnak * XNAO) / (xki + prnak * xnai));
   double xs1ss = 1.0 / (1.0 + exp(-(v - 1.500) / 16.700));
   double tauxs = 1.00 / (0.0000719 * (v + 30.00) / (1.00 - exp(-0.1480 * (v + 30.0))) +
@@ -139,7 +157,7 @@ __host__ __device__ inline void membrane_update(rh_membrane& m, double dt, const
   double fnak = 1.00 / (1.0 + 0.1245 * exp(-0.1 * v * FRT) + 0.0365 * sigma * exp(-v * FRT));
   double xinak = 1. * 1.5000 * fnak * (1.0 / (1.0 + pow((12.00 / xnai), 1.00))) * xko / (xko + 1.50);
   // stimulus (:689-692)
-  double stim = stimulus(c, fmod(t + tperid - 100, tperid));
+  double stim = stimulus(c, t, c.iso ? fmod(t, tperid) : fmod(t + tperid - 100, tperid));
   // [Na]i and V (:701-738)
   double wcainv = 1.0 / 50.0;
   double conv = 0.18 * 12500;
@@ -205,7 +223,7 @@ __host__ __device__ inline bool step_coef(StepCoef<double>& k, const rh_membrane
   k.ncx_den2 = 1.0 + KSAT * e2;
   k.svica = c.svica;
   k.svncx = c.svncx;
-  k.sviup = c.sviup_tot;
+  option_coef(k, c, v, t, dt, fmod(t + 10 * c.pcl, 15.5 * c.pcl));
   k.cao = c.cao;
   k.ku = c.ku;
   k.ku2 = c.ku2;

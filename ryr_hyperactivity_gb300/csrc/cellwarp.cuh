@@ -139,11 +139,11 @@ struct WarpSlots {
 // Membrane step (membrane_update, cellmodel.cuh) by one warp.  `s` is 160
 // doubles of shared memory owned by the warp.  The lattice sums come in as
 // tot (sum cs, sum xicat, sum xinaca over the cell's CRUs, :447-456); the
-// function also computes the three fmods of this step (stimulus phase and the
-// next lattice update's window flags: reset, output, and the two cadist
-// conditions) into fm[0..4].
+// function also computes the fmods of this step (stimulus phase and the next
+// lattice update's window flags: reset, output, the two cadist conditions
+// and the iso LCC phase) into fm[0..5].
 __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const CellConst& c,
-                                            const double tot[3], double* s, double fm[5]) {
+                                            const double tot[3], double* s, double fm[6]) {
   const double tperid = c.pcl, svikr = c.svikr;
   const int nin = c.n;
   const int lane = threadIdx.x & 31;
@@ -182,15 +182,19 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   const double pw = pow(lane == 0 ? q28 : q12, lane == 0 ? 3.0 : 1.00);
   const double pow_ks = __shfl_sync(0xffffffffu, pw, 0);
   const double pow_nak = __shfl_sync(0xffffffffu, pw, 1);
-  // fmods: stimulus phase (:689) and the next update's window, output and
-  // cadist flags (:1244, :777, :1002)
+  // fmods: stimulus phase (:689, iso :683) and the next update's window,
+  // output, cadist and iso LCC flags (:1244, :777, :1002, :1213)
   {
     const double tn = t + dt;
-    const double x = lane == 0 ? t + tperid - 100 : (lane == 1 ? tn - dt : tn + 0.0000001);
-    const double y = lane == 0 ? tperid : lane == 3 ? 5.0 : lane == 4 ? tperid : OUTT;
+    const double x = lane == 0 ? (c.iso ? t : t + tperid - 100)
+                   : lane == 1 ? tn - dt
+                   : lane == 5 ? tn + 10 * tperid
+                               : tn + 0.0000001;
+    const double y = lane == 0 ? tperid : lane == 3 ? 5.0 : lane == 4 ? tperid
+                   : lane == 5 ? 15.5 * tperid : OUTT;
     const double f = fmod(x, y);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) fm[i] = __shfl_sync(0xffffffffu, f, i);
+    for (int i = 0; i < 6; ++i) fm[i] = __shfl_sync(0xffffffffu, f, i);
   }
 
   // ---- round 1: the voltage exponentials, one per lane ----
@@ -228,7 +232,7 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   w.put(4, 0.000610 * (v + 10.00), E[11] - 1.00);              // xkrv2
   w.put(5, 1.00, 1.00 + E[12]);                                // xkrinf
   w.put(6, 1.00, 1.00 + E[13]);                                // rg
-  w.put(7, 0.8, 1 + pow_ks);                                   // qks_inf term
+  w.put(7, c.slowncx ? 1.6 : 0.8, 1 + pow_ks);                 // qks_inf term (:537, :541)
   w.put(8, 1.0, 1.0 + E[14]);                                  // xs1ss
   w.put(9, 0.0000719 * (v + 30.00), 1.00 - E[15]);             // tauxs term 1
   w.put(10, 0.0001310 * (v + 30.00), E[16] - 1.00);            // tauxs term 2
@@ -266,7 +270,7 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   const double tauxs_sum = w.get(9) + w.get(10);
 
   // ---- round 3: second-level divisions ----
-  const double tauqks = 1000.00;
+  const double tauqks = c.slowncx ? 2000 : 1000.00;  // :538, :542
   w.open(11);
   w.put(0, 1.00, ah + bh);                                     // tauh
   w.put(1, 1.00, aj + bj);                                     // tauj
@@ -331,7 +335,7 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   const double xitof = 1.0 * 0.10 * m.xtof * m.ytof * (v - ek);
   m.xtof = xtos_inf - (xtos_inf - m.xtof) * G[7];
   m.ytof = ytos_inf - (ytos_inf - m.ytof) * G[8];
-  const double stim = stimulus(c, fm[0]);
+  const double stim = stimulus(c, t, fm[0]);
   const double wcainv = 1.0 / 50.0;
   const double conv = 0.18 * 12500;
   const double xrr = 1.0 * (1.0 / wcainv / conv) / 1000.0;
@@ -354,10 +358,10 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
 }
 
 // Coefficients of the next lattice update (step_coef, cellmodel.cuh) by one
-// warp; fm holds fmod(t - dt, OUTT), fmod(t + 1e-7, OUTT), fmod(t + 1e-7, 5)
-// and fmod(t + 1e-7, PCL) for the state's time t (entries 1..4 of
-// membrane_update_warp's fm); `s` is 96 doubles of shared memory owned by the
-// warp.  Returns whether the cell is inside its protocol.
+// warp; fm holds fmod(t - dt, OUTT), fmod(t + 1e-7, OUTT), fmod(t + 1e-7, 5),
+// fmod(t + 1e-7, PCL) and fmod(t + 10 PCL, 15.5 PCL) for the state's time t
+// (entries 1..5 of membrane_update_warp's fm); `s` is 96 doubles of shared
+// memory owned by the warp.  Returns whether the cell is inside its protocol.
 __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
                                       const CellConst& c, double dt, const double* fm,
                                       double* s) {
@@ -450,7 +454,7 @@ __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
   k.ncx_den2 = 1.0 + KSAT * e2;
   k.svica = c.svica;
   k.svncx = c.svncx;
-  k.sviup = c.sviup_tot;
+  option_coef(k, c, v, t, dt, fm[4]);
   k.cao = c.cao;
   k.ku = c.ku;
   k.ku2 = c.ku2;

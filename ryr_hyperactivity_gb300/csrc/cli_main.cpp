@@ -20,6 +20,9 @@
 //                                              vclamp holds a3 mV after 100 ms,
 //                                              apclamp reads v_1000.txt (:383-395)
 //   --perm                                     permeabilised-cell build (:35)
+//   --iso --randomlcc --slowncxchange          the -Diso, -Drandomlcc and
+//                                              -Dslowncxchange builds (:31-32, :52)
+//   --ncx ncx|oldncx|ncx_noallo                NCX function (subroutine_cuda.c:47-120)
 //   --mixed                                    FP32 lattice / FP64 whole-cell
 //   --seed S --ikr-scale X --cao MM --linescan-jz J --max-steps N
 #include <stdio.h>
@@ -35,7 +38,8 @@
 static void usage() {
   fprintf(stderr,
           "usage: cuda_Cell_Detailed <device> <name> a3 a4 a5 a6 a7 a8 a9 a10 [--nx N] [--ny N] "
-          "[--nz N] [--nbeats N] [--pcl MS] [--lqt 0|1] [--iso2 0|1] [--tapsi 0|1] [--cadist] [--protocol P] [--perm] [--mixed] "
+          "[--nz N] [--nbeats N] [--pcl MS] [--lqt 0|1] [--iso2 0|1] [--tapsi 0|1] [--cadist] [--protocol P] [--perm] [--iso] [--randomlcc] "
+          "[--slowncxchange] [--ncx F] [--mixed] "
           "[--seed S] [--ikr-scale X] [--cao MM] [--linescan-jz J] [--max-steps N]\n");
 }
 
@@ -80,6 +84,19 @@ int main(int argc, char** argv) {
     else if (k == "--mixed") o.precision = RH_MIXED;
     else if (k == "--cadist") o.record_cadist = 1;
     else if (k == "--perm") p.perm = 1;
+    else if (k == "--iso") p.iso = 1;
+    else if (k == "--randomlcc") p.randomlcc = 1;
+    else if (k == "--slowncxchange") p.slowncx = 1;
+    else if (k == "--ncx") {
+      const std::string v = next();
+      if (v == "ncx") p.ncx_form = RH_NCX_ALLOSTERIC;
+      else if (v == "oldncx") p.ncx_form = RH_NCX_OLD;
+      else if (v == "ncx_noallo") p.ncx_form = RH_NCX_NOALLO;
+      else {
+        usage();
+        return 2;
+      }
+    }
     else if (k == "--protocol") {
       const std::string v = next();
       if (v == "paced") p.protocol = RH_PROTO_PACED;

@@ -75,6 +75,8 @@ struct CellConst {
   double clamp_mv;     // RH_PROTO_VCLAMP holding voltage
   const double* apv;   // RH_PROTO_AP_CLAMP waveform (device), napv samples
   int napv;
+  int iso, randomlcc, slowncx, ncx_form;  // build options (rh_cell_params)
+  double sviup_iso;    // SERCA prefactor once iso is active (t >= 5.5 PCL)
 };
 
 // Mutable per-cell state, owned by the device between host calls.

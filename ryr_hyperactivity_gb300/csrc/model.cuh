@@ -57,6 +57,13 @@ constexpr double KMNAI = 12.3;
 constexpr double KMNAO = 87.5;
 constexpr double KSAT = 0.27;
 constexpr double ETA = 0.35;
+constexpr double KDA = 0.0003;  // mM, Ka of oldncx and ncx_noallo (subroutine_cuda.c:12)
+// oldncx allosteric on/off rates (subroutine_cuda.c:79-80)
+constexpr double KNCXOFF_OLD = 0.00005;
+constexpr double KNCXON_OLD = 2.53e-3 * 0.05;
+// slowncxchange background current, cuda_Cell_Detailed.cu:1268:
+//   bcgcur = BCG_G * (v - log(180000 / cs) / 2 / frt)
+constexpr double BCG_G = 1.0 * 0.003016 / 32.;
 constexpr double FARAD = 96.485;
 constexpr double XRGAS = 8.314;
 constexpr double TEMPER = 308;
@@ -231,7 +238,11 @@ struct StepCoef {
   R lcc_e2z_k, lcc_k;
   // NCX (subroutine_cuda.c:47-75) with za and [Na]i fixed:
   //   Inaca = Ka * (num_a - num_b cs) / ((t1 + t2(cs) + t3a + cs XNAO^3) den2)
-  R ncx_num_a, ncx_num_b, ncx_t1, ncx_t3a, ncx_den2;
+  // t2 = KMNAO^3 cs (1 + cs/KMCAI), or in oldncx/ncx_noallo
+  // KMNAO^3 cs + ncx_t2b (1 + cs/KMCAI) with ncx_t2b = KMNAI^3 Cext (:91, :116)
+  R ncx_num_a, ncx_num_b, ncx_t1, ncx_t3a, ncx_den2, ncx_t2b;
+  // slowncxchange background current: bcgcur = bcg_a - bcg_b log(180000/cs)
+  R bcg_a, bcg_b;
   // cell parameters
   R svica, svncx, sviup, cao, ku, ku2, kb;
   // time step constants
@@ -240,6 +251,10 @@ struct StepCoef {
   int output_step;   // fmod(t+1e-7, outt) < dt (:777)
   int cadist_step;   // output step that also writes a cadist record (:1002)
   int perm;          // permeabilised cell: no LCC/NCX, [Ca] faces held (-Dperm)
+  int ncx_form;      // RH_NCX_*
+  int ncx_ka_hill;   // ncx_noallo below -75 mV: Ka = 1/(1+(Kda/cs)^3), else 1 (:110-112)
+  int slowncx;       // slowncxchange: bcgcur on, allosteric Ka = 5 Ancx
+  int iso_add_lcc;   // iso: fill the empty LCC slots 4-7 this step (:1213-1218)
 };
 
 template <class R, class Q>
@@ -247,13 +262,18 @@ __host__ __device__ inline void convert_coef(StepCoef<R>& d, const StepCoef<Q>& 
   d.alphac = R(s.alphac); d.betac = R(s.betac); d.alphad = R(s.alphad); d.betad = R(s.betad);
   d.alphaf = R(s.alphaf); d.betaf = R(s.betaf); d.lcc_e2z_k = R(s.lcc_e2z_k); d.lcc_k = R(s.lcc_k);
   d.ncx_num_a = R(s.ncx_num_a); d.ncx_num_b = R(s.ncx_num_b); d.ncx_t1 = R(s.ncx_t1);
-  d.ncx_t3a = R(s.ncx_t3a); d.ncx_den2 = R(s.ncx_den2); d.svica = R(s.svica); d.svncx = R(s.svncx);
+  d.ncx_t3a = R(s.ncx_t3a); d.ncx_den2 = R(s.ncx_den2); d.ncx_t2b = R(s.ncx_t2b);
+  d.bcg_a = R(s.bcg_a); d.bcg_b = R(s.bcg_b); d.svica = R(s.svica); d.svncx = R(s.svncx);
   d.sviup = R(s.sviup); d.cao = R(s.cao); d.ku = R(s.ku); d.ku2 = R(s.ku2); d.kb = R(s.kb);
   d.dt = R(s.dt); d.rdt = R(s.rdt); d.dth = R(s.dth); d.rdt95 = R(s.rdt95); d.rdth95 = R(s.rdth95);
   d.reset_window = s.reset_window;
   d.output_step = s.output_step;
   d.cadist_step = s.cadist_step;
   d.perm = s.perm;
+  d.ncx_form = s.ncx_form;
+  d.ncx_ka_hill = s.ncx_ka_hill;
+  d.slowncx = s.slowncx;
+  d.iso_add_lcc = s.iso_add_lcc;
 }
 
 // ---- RyR transition draw (subroutine_cuda.c:332-363 and siblings) ----

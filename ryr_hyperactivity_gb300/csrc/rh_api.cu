@@ -363,6 +363,10 @@ void rh_default_cell_params(rh_cell_params* p) {
   p->linescan_jz = -1;
   p->protocol = RH_PROTO_PACED;
   p->perm = 0;
+  p->iso = 0;
+  p->randomlcc = 0;
+  p->slowncx = 0;
+  p->ncx_form = RH_NCX_ALLOSTERIC;
 }
 
 void rh_default_run_opts(rh_run_opts* o) {
@@ -454,6 +458,16 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     if (p.tapsi) sviup = 0;
     double sviup_lqt = (p.lqt && p.tapsi) ? 0.05 : 0.;
     cc.sviup_tot = sviup + sviup_lqt;
+    // iso doubles SERCA from 5.5 PCL on; iso2 and tapsi still override (:1220-1238)
+    double sviup_iso = p.iso2 ? (1.0 + 0.75) * 1.75 : (1.0 + 0.75) * 2.;
+    if (p.tapsi) sviup_iso = 0;
+    cc.sviup_iso = sviup_iso + sviup_lqt;
+    if (p.ncx_form < RH_NCX_ALLOSTERIC || p.ncx_form > RH_NCX_NOALLO)
+      return fail(s, RH_ERR_ARG, "cell %d: unknown NCX form %d", c, p.ncx_form);
+    cc.iso = p.iso ? 1 : 0;
+    cc.randomlcc = p.randomlcc ? 1 : 0;
+    cc.slowncx = p.slowncx ? 1 : 0;
+    cc.ncx_form = p.ncx_form;
     cc.svikr = p.lqt ? 0 : 3 * p.ikr_scale;
     cc.cao = p.cao_mM;
     cc.ku = p.ku;

@@ -82,7 +82,7 @@ __noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool ou
   rh_membrane m = dyn->m;
   const double dt = a.dt;
   // reduction (:447-456) and membrane model (:458-739), warp-parallel
-  double fm[5];
+  double fm[6];
   membrane_update_warp(m, dt, cc, tot, scratch, fm);
   uint32_t status = dyn->status;
   if (!isfinite(m.v) || !isfinite(m.xnai) || !isfinite(m.csubt) || !isfinite(m.xicatto) ||
@@ -426,6 +426,13 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       R qq = Math<R>::div(R(25), cpx);
       bfca = Math<R>::div(R(0.175), R(1) + qq * qq);
     }
+    if (k.iso_add_lcc) {  // iso: the empty slots 4-7 receive a channel in state 3 (:1213-1218)
+      uint32_t hi = lccw.y;
+#pragma unroll
+      for (int b = 0; b < 32; b += 8)
+        if (((hi >> b) & 0xffu) == 16u) hi = (hi & ~(0xffu << b)) | (3u << b);
+      lccw.y = hi;
+    }
     int nlcp = 0;
     if (!k.perm) {  // a permeabilised cell has no LCC current (:1249-1263 under -Dperm)
       uint64_t slots = ((uint64_t)lccw.y << 32) | lccw.x;
@@ -463,19 +470,43 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     R xire = R(0.0147 * SVJMAX) * po * (cjsr - cp) * R(1.0 / VP);
     if (xire < R(0)) xire = R(0);
 
-    // ---- NCX (:1296, subroutine_cuda.c:47-75); none in a permeabilised cell,
-    //      whose xinaca keeps its initial 0 and Ancx its value (:1294-1300) ----
+    // ---- NCX (:1296, subroutine_cuda.c:47-120); zero in a permeabilised
+    //      cell, whose Ancx keeps its value (:1302) ----
     R xinaca = R(0);
     if (!k.perm) {
       const R csm = cs0 * R(1e-3);
-      const R t2 = R(KMNAO * KMNAO * KMNAO) * csm * (R(1) + csm * R(1.0 / KMCAI));
       const R t3 = k.ncx_t3a + csm * R(XNAO * XNAO * XNAO);
-      const R inaca = Math<R>::div(ancx * R(VNACA) * (k.ncx_num_a - k.ncx_num_b * csm),
-                                   (k.ncx_t1 + t2 + t3) * k.ncx_den2);
-      const R r3 = Math<R>::div(R(0.0003), csm);
-      ancx += (Math<R>::div(R(1), R(1) + r3 * r3 * r3) - ancx) * R(1.0 / 150.) * dt;
-      xinaca = k.svncx * inaca;
+      if (k.ncx_form == RH_NCX_ALLOSTERIC) {  // ncx, :47-75
+        const R t2 = R(KMNAO * KMNAO * KMNAO) * csm * (R(1) + csm * R(1.0 / KMCAI));
+        const R ka = k.slowncx ? ancx * R(5) : ancx;  // slowncxchange: Ka = 5 Ancx (:59-62)
+        const R inaca = Math<R>::div(ka * R(VNACA) * (k.ncx_num_a - k.ncx_num_b * csm),
+                                     (k.ncx_t1 + t2 + t3) * k.ncx_den2);
+        const R r3 = Math<R>::div(R(0.0003), csm);
+        ancx += (Math<R>::div(R(1), R(1) + r3 * r3 * r3) - ancx) * R(1.0 / 150.) * dt;
+        xinaca = k.svncx * inaca;
+      } else {  // oldncx (:77-100) and ncx_noallo (:102-120)
+        R ka = R(1);
+        if (k.ncx_ka_hill) {
+          const R q = Math<R>::div(R(KDA), csm);
+          ka = Math<R>::div(R(1), R(1) + q * q * q);
+        }
+        const R t2 = R(KMNAO * KMNAO * KMNAO) * csm + k.ncx_t2b * (R(1) + csm * R(1.0 / KMCAI));
+        const R inaca = Math<R>::div(ka * R(VNACA) * (k.ncx_num_a - k.ncx_num_b * csm),
+                                     (k.ncx_t1 + t2 + t3) * k.ncx_den2);
+        if (k.ncx_form == RH_NCX_OLD) {  // allosteric state from on/off rates, capped
+          const R cu = csm * R(1000);
+          const R on = R(KNCXON_OLD) * cu * cu;
+          R da = on * (R(1) - ancx) - ancx * R(KNCXOFF_OLD);
+          if (on * dt > R(0.95)) da = k.rdt95 * (R(1) - ancx) - ancx * R(KNCXOFF_OLD);
+          ancx += da * dt;
+        }
+        xinaca = k.svncx * inaca;
+      }
     }
+    // slowncxchange background Ca current (:1267-1269), into xicat and the
+    // submembrane balance
+    R bcgcur = R(0);
+    if (k.slowncx) bcgcur = k.bcg_a - k.bcg_b * Math<R>::log(Math<R>::div(R(180000), cs0));
 
     // ---- CSQN buffering of the JSR (:1316-1317) ----
     const R beta = csqn_beta<R>(cjsr, roo2, mono);
@@ -498,7 +529,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       const R csdiff = (csN + csS - R(2) * cs0) * R(1.0 / TAUST);
       const R cs_const = -R(ICAGAMMA * VP / VS) * icat1 + xinaca -
                          (cs0 - ci0) * R(1.0 / TAUSI / 2.) - (cs0 - ci1) * R(1.0 / TAUSI / 2.) +
-                         csdiff;
+                         csdiff - bcgcur;
       const R cp_const =
           (ci0 - cp) * R(1.0 / TAUPI / 2.) + (ci1 - cp) * R(1.0 / TAUPI / 2.) + xire - icat1;
 #pragma unroll 1
@@ -541,7 +572,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       a.diag[(int64_t)D_XIRE * S + g] = (double)xire;
       a.diag[(int64_t)D_PO * S + g] = (double)po;
       a.diag[(int64_t)D_XINACA * S + g] = (double)xinaca;
-      a.diag[(int64_t)D_XICAT * S + g] = (double)icat1;
+      a.diag[(int64_t)D_XICAT * S + g] = (double)(icat1 + bcgcur * R(VS / VP));
     }
     tstat = status;
 
@@ -775,7 +806,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     }
 
     p_cs = csn;
-    p_xicat = icat1;
+    p_xicat = icat1 + bcgcur * R(VS / VP);  // xicat (:1271)
     p_xinaca = xinaca;
 
     if (OUT && out_step) {
@@ -958,7 +989,18 @@ __global__ void init_kernel(Lattice<R> L, const CellConst* cells, const InitValu
     }
     L.ryr[g] = (uint32_t)v.nou | ((uint32_t)v.ncu << 8) | ((uint32_t)v.nob << 16) |
                ((uint32_t)v.ncb << 24);
-    L.lcc[g] = make_uint2(v.lcc_lo, v.lcc_hi);
+    uint2 lcc = make_uint2(v.lcc_lo, v.lcc_hi);
+    if (c.randomlcc) {  // 0..8 channels: curand() % 9 at initialisation (:1150-1151)
+      const int x = q % c.lx, y = (q / c.lx) % c.ly, z = q / (c.lx * c.ly);
+      const uint32_t pos = (uint32_t)((x + 1) + c.nxf * ((y + 1) + c.nyf * (z + 1)));
+      rh_stream rng;
+      rh_stream_init(&rng, c.seed, c.cell_id, pos, RH_PHILOX_INIT_STEP);
+      const uint32_t nlcc = rh_uniform_u32(&rng) % 9u;
+      uint64_t slots = 0;
+      for (uint32_t ll = 0; ll < 8; ++ll) slots |= (uint64_t)(ll < nlcc ? 3u : 16u) << (8 * ll);
+      lcc = make_uint2((uint32_t)slots, (uint32_t)(slots >> 32));
+    }
+    L.lcc[g] = lcc;
     L.win[g] = 0;
   }
 }

@@ -14,8 +14,9 @@ Fixtures (all produced by running the reference's own code):
                                      run for CADIST_STEPS steps (its sha256 is in
                                      ref_full_runs.json under "small_il_cd")
 
-The protocol builds (vclamp, brownvclamp, apclamp, linearapclamp, nopacing,
-perm) are recorded in ref_full_runs.json only: the first wholetest_ line as
+The protocol and option builds (vclamp, brownvclamp, apclamp, linearapclamp,
+nopacing, perm, iso, iso_il, slowncxchange, oldncx, ncx_noallo) are recorded
+in ref_full_runs.json only: the first wholetest_ line as
 text (in some of these builds it carries the reference's uninitialised
 window accumulators, cuda_Cell_Detailed.cu:332-334), the sha256 of the rest
 of the file and of the linescan_ file.  The apclamp build reads the waveform
@@ -70,6 +71,23 @@ PROTOCOL_RUNS = {
     "perm": dict(args=CONTROL[:7] + [2],
                  cell=dict(nx=12, ny=9, nz=6, nbeats=1, pcl_ms=1000.0, lqt=0, iso2=0,
                            linescan_jz=-1, perm=1), steps=6000),
+    # iso through the LCC insertion and SERCA boost at 5.5 PCL and the end of
+    # pacing at 11.9 PCL
+    "iso": dict(args=CONTROL,
+                cell=dict(nx=8, ny=6, nz=5, nbeats=13, pcl_ms=100.0, lqt=0, iso2=0,
+                          linescan_jz=-1, iso=1), steps=52000),
+    "iso_il": dict(args=CONTROL,
+                   cell=dict(nx=8, ny=6, nz=5, nbeats=13, pcl_ms=100.0, lqt=1, iso2=1,
+                             linescan_jz=-1, iso=1), steps=30000),
+    "slowncxchange": dict(args=CONTROL,
+                          cell=dict(nx=12, ny=8, nz=5, nbeats=1, pcl_ms=400.0, lqt=0, iso2=0,
+                                    linescan_jz=-1, slowncx=1), steps=12000),
+    "oldncx": dict(args=CONTROL,
+                   cell=dict(nx=12, ny=8, nz=5, nbeats=1, pcl_ms=400.0, lqt=0, iso2=0,
+                             linescan_jz=-1, ncx_form="oldncx"), steps=12000),
+    "ncx_noallo": dict(args=CONTROL,
+                       cell=dict(nx=12, ny=8, nz=5, nbeats=1, pcl_ms=400.0, lqt=0, iso2=0,
+                                 linescan_jz=-1, ncx_form="ncx_noallo"), steps=12000),
 }
 CADIST_VARIANT = "small_il_cd"  # small_il with the cadist_ writer enabled
 CADIST_STEPS = 1700

@@ -20,7 +20,8 @@ pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 META = json.load(open(os.path.join(GOLD, "ref_full_runs.json")))
-VARIANTS = ["vclamp", "brownvclamp", "apclamp", "linearapclamp", "nopacing", "perm"]
+VARIANTS = ["vclamp", "brownvclamp", "apclamp", "linearapclamp", "nopacing", "perm", "iso",
+            "iso_il", "slowncxchange", "oldncx", "ncx_noallo"]
 EXE = os.path.join(os.path.dirname(os.path.dirname(__file__)), "ryr_hyperactivity_gb300", "bin",
                    "cuda_Cell_Detailed")
 
@@ -79,6 +80,28 @@ def test_protocols_in_one_batch():
                                        err_msg=f"cell {c}")
 
 
+def test_randomlcc_cells_match_their_oracles():
+    """randomlcc: every CRU starts with 0..8 LCCs from one Philox draw (the
+    reference's own draw reads an uninitialised curand state, :1150 runs
+    before setup_kernel, so this draw is defined here).  GPU and oracle give
+    the same channel layout and follow each other; all nine counts occur."""
+    cells = [c1_params(nx=14, ny=9, nz=6, seed=11, cell_id=i, randomlcc=1, iso=i, pcl_ms=100.0,
+                       nbeats=13) for i in range(2)]
+    steps = 4000
+    with Simulator(cells, precision="fp64") as sim:
+        st0 = [sim.get_state(c) for c in range(2)]
+        sim.run_steps(steps)
+        for c, p in enumerate(cells):
+            o = O.Oracle(p)
+            ref0 = o.get_state()
+            np.testing.assert_array_equal(st0[c]["lcc"], ref0["lcc"])
+            n = (st0[c]["lcc"].reshape(8, -1) < 16).sum(axis=0)
+            assert set(np.unique(n)) == set(range(9))
+            _, wc_ref, _ = o.run(steps)
+            np.testing.assert_allclose(sim.drain_wholecell(c), wc_ref, rtol=1e-9, atol=1e-9)
+            np.testing.assert_array_equal(sim.get_state(c)["lcc"], o.get_state()["lcc"])
+
+
 def test_mixed_precision_protocols_run():
     """The mixed path runs the protocols too: a voltage clamp holds V exactly,
     and the records are finite where the FP64 ones are (two wholecell ratio
@@ -113,7 +136,7 @@ def test_ap_clamp_waveform_is_required_and_checked():
             sim.set_ap_clamp(0, ap_waveform(400.0))
 
 
-@pytest.mark.parametrize("variant", ["vclamp", "apclamp", "perm"])
+@pytest.mark.parametrize("variant", ["vclamp", "apclamp", "perm", "iso", "slowncxchange", "oldncx"])
 def test_cli_protocol_builds(variant):
     """The drop-in program's --protocol / --perm options write the files the
     reference's protocol builds write (numerically equal to the oracle's;
@@ -131,6 +154,12 @@ def test_cli_protocol_builds(variant):
         flags += ["--protocol", c["protocol"]]
     if c.get("perm"):
         flags += ["--perm"]
+    if c.get("iso"):
+        flags += ["--iso"]
+    if c.get("slowncx"):
+        flags += ["--slowncxchange"]
+    if "ncx_form" in c:
+        flags += ["--ncx", c["ncx_form"]]
     with tempfile.TemporaryDirectory() as d:
         if variant == "apclamp":
             with open(os.path.join(d, "v_1000.txt"), "w") as f:

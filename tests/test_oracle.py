@@ -58,14 +58,16 @@ def test_oracle_cadist_matches_reference():
 # (:1044-1045, :1058): the reference leaves them uninitialised before the first
 # output window (:332-334), the oracle starts them at 0
 WINDOW_COLS = (3, 4, 17)
-PROTOCOL_VARIANTS = ["vclamp", "brownvclamp", "apclamp", "linearapclamp", "nopacing", "perm"]
+PROTOCOL_VARIANTS = ["vclamp", "brownvclamp", "apclamp", "linearapclamp", "nopacing", "perm",
+                     "iso", "iso_il", "slowncxchange", "oldncx", "ncx_noallo"]
 
 
 @pytest.mark.parametrize("variant", PROTOCOL_VARIANTS)
 def test_oracle_matches_reference_protocol_build(variant):
-    """The voltage protocols and the permeabilised cell against the reference
-    built with the matching switch: every wholetest_ and linescan_ byte,
-    except the first record's uninitialised window accumulators."""
+    """The voltage protocols, the permeabilised cell, isoproterenol,
+    slowncxchange and the two unused NCX forms against the reference built
+    with the matching switch: every wholetest_ and linescan_ byte, except the
+    first record's uninitialised window accumulators."""
     from tests.gpu_helpers import ap_waveform, variant_params
     spec = META[variant]
     p = variant_params(spec)
