@@ -15,6 +15,8 @@
 //   --nx N --ny N --nz N --nbeats N --pcl MS   lattice and protocol
 //   --lqt 0|1 --iso2 0|1 --tapsi 0|1           build modes (Makefile:8-28)
 //   --cadist                                   outputcadist build (:1001-1013)
+//   --no-linescan                              build without outputlinescan (:46):
+//                                              linescan_<name> stays empty
 //   --protocol paced|nopacing|vclamp|brownvclamp|apclamp|linearapclamp
 //                                              voltage protocol build (:34, :54-61);
 //                                              vclamp holds a3 mV after 100 ms,
@@ -38,7 +40,7 @@
 static void usage() {
   fprintf(stderr,
           "usage: cuda_Cell_Detailed <device> <name> a3 a4 a5 a6 a7 a8 a9 a10 [--nx N] [--ny N] "
-          "[--nz N] [--nbeats N] [--pcl MS] [--lqt 0|1] [--iso2 0|1] [--tapsi 0|1] [--cadist] [--protocol P] [--perm] [--iso] [--randomlcc] "
+          "[--nz N] [--nbeats N] [--pcl MS] [--lqt 0|1] [--iso2 0|1] [--tapsi 0|1] [--cadist] [--no-linescan] [--protocol P] [--perm] [--iso] [--randomlcc] "
           "[--slowncxchange] [--ncx F] [--mixed] "
           "[--seed S] [--ikr-scale X] [--cao MM] [--linescan-jz J] [--max-steps N]\n");
 }
@@ -83,6 +85,7 @@ int main(int argc, char** argv) {
     else if (k == "--tapsi") p.tapsi = atoi(next());
     else if (k == "--mixed") o.precision = RH_MIXED;
     else if (k == "--cadist") o.record_cadist = 1;
+    else if (k == "--no-linescan") o.record_linescan = 0;
     else if (k == "--perm") p.perm = 1;
     else if (k == "--iso") p.iso = 1;
     else if (k == "--randomlcc") p.randomlcc = 1;

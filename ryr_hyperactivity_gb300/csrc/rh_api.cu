@@ -485,7 +485,7 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     if (p.protocol == RH_PROTO_AP_CLAMP && cc.napv < 1)
       return fail(s, RH_ERR_ARG, "cell %d: AP clamp needs pcl_ms >= dt", c);
     off += (n64 + 31) & ~int64_t(31);
-    ls_off += (int64_t)s->opts.output_capacity * cc.lx;
+    if (s->opts.record_linescan) ls_off += (int64_t)s->opts.output_capacity * cc.lx;
     if (s->opts.record_cadist)
       cd_off += (int64_t)s->opts.cadist_capacity * (2 + RH_CADIST_COLS * n64);
     s->max_n = std::max(s->max_n, cc.n);
@@ -570,7 +570,8 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   CK(cudaMalloc(&s->d_partials, sizeof(double) * P_COUNT * (size_t)max_tiles));
   CK(cudaMalloc(&s->d_out_wc, sizeof(double) * RH_WHOLECELL_COLS * (size_t)ncells *
                                   s->opts.output_capacity));
-  CK(cudaMalloc(&s->d_out_ls, sizeof(double) * RH_LINESCAN_COLS * (size_t)std::max<int64_t>(ls_off, 1)));
+  if (s->opts.record_linescan)  // the reference's outputlinescan switch (:46, :967)
+    CK(cudaMalloc(&s->d_out_ls, sizeof(double) * RH_LINESCAN_COLS * (size_t)std::max<int64_t>(ls_off, 1)));
   if (s->opts.record_cadist) {
     if (cudaMalloc(&s->d_out_cd, sizeof(double) * (size_t)cd_off) != cudaSuccess) {
       cudaGetLastError();
@@ -997,6 +998,8 @@ int rh_drain_linescan(rh_sim* s, int32_t cell, double* rows, int32_t max_rec, in
   int r = check_cell(s, cell);
   if (r) return r;
   if (!nrec || max_rec < 0 || (max_rec > 0 && !rows)) return RH_ERR_ARG;
+  *nrec = 0;
+  if (!s->d_out_ls) return RH_OK;  // record_linescan off: no rows
   CK(cudaSetDevice(s->device));
   CellDyn d;
   if ((r = read_dyn(s, cell, &d))) return r;

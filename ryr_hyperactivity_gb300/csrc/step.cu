@@ -863,7 +863,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         r[4] = (double)xinaca;  // scaled on the host as the reference prints it
         r[5] = (double)xire;
       }
-      if (y == sh.line_y && z == sh.line_z) {  // linescan row (:967-989), post-step values
+      if (a.out_ls && y == sh.line_y && z == sh.line_z) {  // linescan row (:967-989), post-step values
         const int64_t g0 = g;
         double* r = a.out_ls + ((size_t)sh.ls_off + (size_t)sh.slot * lx + x) * RH_LINESCAN_COLS;
         r[0] = sh.t;

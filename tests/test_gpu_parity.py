@@ -367,3 +367,16 @@ def test_cli_cadist_file_is_the_reference_file():
         text = open(os.path.join(d, "cadist_cd")).read()
     assert text.count("header") == spec["cadist_records"]
     assert hashlib.sha256(text.encode()).hexdigest() == spec["cadist_sha256"]
+
+
+def test_linescan_off_changes_nothing_else():
+    """record_linescan = 0 (the reference built without outputlinescan, :46)
+    drains no linescan rows and leaves every other output bit-identical."""
+    p = c1_params(nx=12, ny=8, nz=5)
+    out = []
+    for ls in (1, 0):
+        with Simulator(p, precision="mixed", record_linescan=ls) as sim:
+            sim.run_steps(1000)
+            out.append((sim.drain_wholecell(0), sim.drain_linescan(0)))
+    assert len(out[0][1]) == 10 and len(out[1][1]) == 0
+    np.testing.assert_array_equal(out[0][0], out[1][0])
