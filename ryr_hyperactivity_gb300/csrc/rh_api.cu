@@ -45,6 +45,7 @@ struct rh_sim {
   // updates they run) overlaps the other groups' lattice work.
   int ngroups = 1;
   std::vector<int> group_cell;  // group g holds cells [group_cell[g], group_cell[g+1])
+  std::vector<char> group_opt;  // group g has a cell with lattice build options
   std::vector<cudaStream_t> gstreams;
   std::vector<cudaEvent_t> gevents;  // [0] fork, [1..G] join
   int64_t stride = 0;
@@ -241,12 +242,12 @@ cudaError_t launch_group(rh_sim* s, int g, bool out, bool lattice_only, cudaStre
     StepArgs<float> a = make_args(s, s->Lf, lattice_only);
     a.tiles += tb;
     a.tile_base = tb;
-    return launch_step<float>(a, te - tb, out, t.tile, st);
+    return launch_step<float>(a, te - tb, out, s->group_opt[g], t.tile, st);
   }
   StepArgs<double> a = make_args(s, s->Ld, lattice_only);
   a.tiles += tb;
   a.tile_base = tb;
-  return launch_step<double>(a, te - tb, out, t.tile, st);
+  return launch_step<double>(a, te - tb, out, s->group_opt[g], t.tile, st);
 }
 
 // `n` steps of every group: group g's launches go to its own stream, forked
@@ -539,6 +540,10 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     }
     s->ngroups = (int)s->group_cell.size();
     s->group_cell.push_back(ncells);
+    s->group_opt.assign(s->ngroups, 0);
+    for (int g = 0; g < s->ngroups; ++g)
+      for (int c = s->group_cell[g]; c < s->group_cell[g + 1]; ++c)
+        if (cell_uses_options(s->hcells[c])) s->group_opt[g] = 1;
     if (s->ngroups > 1) {
       s->gstreams.resize(s->ngroups);
       s->gevents.resize(s->ngroups + 1);

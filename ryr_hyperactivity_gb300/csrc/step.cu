@@ -189,7 +189,7 @@ struct TileHeader {
   int parity, done;
 };
 
-template <class R, bool OUT, int B>
+template <class R, bool OUT, int B, bool OPT>
 __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArgs<R> a) {
   constexpr int kBlock = B;
   using TS = TileSmem<R, B>;
@@ -369,6 +369,12 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
 
   if (valid) {
     const StepCoef<R>& k = sk;
+    // the cell's build options (perm, iso, slowncxchange, NCX form); the
+    // OPT = false variant runs groups whose cells use none of them, with all
+    // of this folded away at compile time
+    const bool o_perm = OPT && k.perm;
+    const bool o_slowncx = OPT && k.slowncx;
+    const int o_ncx = OPT ? k.ncx_form : RH_NCX_ALLOSTERIC;
     const R dt = k.dt;
     const int x = q % lx, y = (q / lx) % ly, z = q / lxly;
     const R* cs = L.cs[par];
@@ -426,7 +432,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       R qq = Math<R>::div(R(25), cpx);
       bfca = Math<R>::div(R(0.175), R(1) + qq * qq);
     }
-    if (k.iso_add_lcc) {  // iso: the empty slots 4-7 receive a channel in state 3 (:1213-1218)
+    if (OPT && k.iso_add_lcc) {  // iso: the empty slots 4-7 receive a channel in state 3 (:1213-1218)
       uint32_t hi = lccw.y;
 #pragma unroll
       for (int b = 0; b < 32; b += 8)
@@ -434,7 +440,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       lccw.y = hi;
     }
     int nlcp = 0;
-    if (!k.perm) {  // a permeabilised cell has no LCC current (:1249-1263 under -Dperm)
+    if (!o_perm) {  // a permeabilised cell has no LCC current (:1249-1263 under -Dperm)
       uint64_t slots = ((uint64_t)lccw.y << 32) | lccw.x;
 #pragma unroll 1
       for (int ll = 0; ll < 8; ++ll) {
@@ -454,7 +460,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       lccw.y = (uint32_t)(slots >> 32);
     }
     R icat1 = R(0);
-    if (!k.perm) {
+    if (!o_perm) {
       R ica = k.lcc_k * (cpx * k.lcc_e2z_k - k.cao);
       if (ica > R(0)) ica = R(0);
       icat1 = k.svica * R(nlcp) * ica;
@@ -473,12 +479,12 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     // ---- NCX (:1296, subroutine_cuda.c:47-120); zero in a permeabilised
     //      cell, whose Ancx keeps its value (:1302) ----
     R xinaca = R(0);
-    if (!k.perm) {
+    if (!o_perm) {
       const R csm = cs0 * R(1e-3);
       const R t3 = k.ncx_t3a + csm * R(XNAO * XNAO * XNAO);
-      if (k.ncx_form == RH_NCX_ALLOSTERIC) {  // ncx, :47-75
+      if (o_ncx == RH_NCX_ALLOSTERIC) {  // ncx, :47-75
         const R t2 = R(KMNAO * KMNAO * KMNAO) * csm * (R(1) + csm * R(1.0 / KMCAI));
-        const R ka = k.slowncx ? ancx * R(5) : ancx;  // slowncxchange: Ka = 5 Ancx (:59-62)
+        const R ka = o_slowncx ? ancx * R(5) : ancx;  // slowncxchange: Ka = 5 Ancx (:59-62)
         const R inaca = Math<R>::div(ka * R(VNACA) * (k.ncx_num_a - k.ncx_num_b * csm),
                                      (k.ncx_t1 + t2 + t3) * k.ncx_den2);
         const R r3 = Math<R>::div(R(0.0003), csm);
@@ -493,7 +499,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         const R t2 = R(KMNAO * KMNAO * KMNAO) * csm + k.ncx_t2b * (R(1) + csm * R(1.0 / KMCAI));
         const R inaca = Math<R>::div(ka * R(VNACA) * (k.ncx_num_a - k.ncx_num_b * csm),
                                      (k.ncx_t1 + t2 + t3) * k.ncx_den2);
-        if (k.ncx_form == RH_NCX_OLD) {  // allosteric state from on/off rates, capped
+        if (o_ncx == RH_NCX_OLD) {  // allosteric state from on/off rates, capped
           const R cu = csm * R(1000);
           const R on = R(KNCXON_OLD) * cu * cu;
           R da = on * (R(1) - ancx) - ancx * R(KNCXOFF_OLD);
@@ -506,7 +512,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     // slowncxchange background Ca current (:1267-1269), into xicat and the
     // submembrane balance
     R bcgcur = R(0);
-    if (k.slowncx) bcgcur = k.bcg_a - k.bcg_b * Math<R>::log(Math<R>::div(R(180000), cs0));
+    if (o_slowncx) bcgcur = k.bcg_a - k.bcg_b * Math<R>::log(Math<R>::div(R(180000), cs0));
 
     // ---- CSQN buffering of the JSR (:1316-1317) ----
     const R beta = csqn_beta<R>(cjsr, roo2, mono);
@@ -522,7 +528,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       const R dth = k.dth, rdth95 = k.rdth95;
       // z faces: zero flux (the ghost repeats cs), or the permeabilised
       // cell's bath value, which its ghosts keep (:1603-1689 under -Dperm)
-      const R cs_face = k.perm ? R(PERM_CI_BASAL) : cs0;
+      const R cs_face = o_perm ? R(PERM_CI_BASAL) : cs0;
       R csN = cs_face, csS = cs_face;
       if (has_zp) csN = kStage ? s_hcs[1][tid] : __ldg(cs + g + lxly);
       if (has_zm) csS = kStage ? s_hcs[0][tid] : __ldg(cs + g - lxly);
@@ -538,7 +544,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         const R r_sarh =
             buffer_rate<R>(R(KSARHON), R(KSARHOFF), R(BSARH), casarh, csn, dth, rdth95);
         R dotcs = R(VP / VS / TAUPS) * (cp - csn) + cs_const - (r_sar + r_sarh);
-        if (k.perm) dotcs += (R(PERM_CI_BASAL) - csn) * R(0.2);  // :1409-1411
+        if (o_perm) dotcs += (R(PERM_CI_BASAL) - csn) * R(0.2);  // :1409-1411
         const R cpbuff = buffer_rate<R>(R(KSARON), R(KSAROFF), R(BSAR), casarj, cp, dth, rdth95);
         const R cpbuffh =
             buffer_rate<R>(R(KSARHON), R(KSARHOFF), R(BSARH), casarhj, cp, dth, rdth95);
@@ -626,7 +632,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         nb5 = mgmyo2[gq];
       }
       // ci a face ghost holds: the sub-voxel's own value, or the bath
-      const V cface = k.perm ? splat2(R(PERM_CI_BASAL)) : c;
+      const V cface = o_perm ? splat2(R(PERM_CI_BASAL)) : c;
       // z
       V czp = c, nzp = n, czm = c, nzm = n;
       if (kStage) {
@@ -1033,11 +1039,12 @@ template <class R, int B>
 cudaError_t opt_in_smem() {
   constexpr size_t smem = TileSmem<R, B>::kBytes;
   if (smem <= 48 * 1024) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(step_kernel<R, true, B>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(step_kernel<R, false, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem);
+  const cudaFuncAttribute attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(step_kernel<R, true, B, false>, attr, (int)smem))) return e;
+  if ((e = cudaFuncSetAttribute(step_kernel<R, false, B, false>, attr, (int)smem))) return e;
+  if ((e = cudaFuncSetAttribute(step_kernel<R, true, B, true>, attr, (int)smem))) return e;
+  return cudaFuncSetAttribute(step_kernel<R, false, B, true>, attr, (int)smem);
 }
 
 cudaError_t prepare_step_kernels() {
@@ -1051,21 +1058,25 @@ cudaError_t prepare_step_kernels() {
 }
 
 template <class R, int B>
-void launch_b(const StepArgs<R>& a, int ntiles, bool out, cudaStream_t st) {
+void launch_b(const StepArgs<R>& a, int ntiles, bool out, bool opt, cudaStream_t st) {
   constexpr size_t smem = TileSmem<R, B>::kBytes;
-  if (out)
-    step_kernel<R, true, B><<<ntiles, B, smem, st>>>(a);
-  else
-    step_kernel<R, false, B><<<ntiles, B, smem, st>>>(a);
+  if (opt) {
+    if (out) step_kernel<R, true, B, true><<<ntiles, B, smem, st>>>(a);
+    else step_kernel<R, false, B, true><<<ntiles, B, smem, st>>>(a);
+  } else {
+    if (out) step_kernel<R, true, B, false><<<ntiles, B, smem, st>>>(a);
+    else step_kernel<R, false, B, false><<<ntiles, B, smem, st>>>(a);
+  }
 }
 
 template <class R>
-cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, int tile, cudaStream_t st) {
+cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, bool opt, int tile,
+                        cudaStream_t st) {
   if (ntiles <= 0) return cudaSuccess;
   switch (tile) {
-    case 64: launch_b<R, 64>(a, ntiles, out, st); break;
-    case 128: launch_b<R, 128>(a, ntiles, out, st); break;
-    case 256: launch_b<R, 256>(a, ntiles, out, st); break;
+    case 64: launch_b<R, 64>(a, ntiles, out, opt, st); break;
+    case 128: launch_b<R, 128>(a, ntiles, out, opt, st); break;
+    case 256: launch_b<R, 256>(a, ntiles, out, opt, st); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -1086,8 +1097,10 @@ cudaError_t launch_volt_prep(const CellConst* cells, CellDyn* dyn, int ncells, d
   return cudaGetLastError();
 }
 
-template cudaError_t launch_step<double>(const StepArgs<double>&, int, bool, int, cudaStream_t);
-template cudaError_t launch_step<float>(const StepArgs<float>&, int, bool, int, cudaStream_t);
+template cudaError_t launch_step<double>(const StepArgs<double>&, int, bool, bool, int,
+                                         cudaStream_t);
+template cudaError_t launch_step<float>(const StepArgs<float>&, int, bool, bool, int,
+                                        cudaStream_t);
 template cudaError_t launch_init<double>(const Lattice<double>&, const CellConst*,
                                          const InitValues*, int, int, cudaStream_t);
 template cudaError_t launch_init<float>(const Lattice<float>&, const CellConst*,

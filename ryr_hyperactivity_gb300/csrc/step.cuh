@@ -36,9 +36,18 @@ struct InitValues {
   uint32_t lcc_lo, lcc_hi;
 };
 
-// One time step with tiles of `tile` CRUs (one of kTileSizes).
+// One time step with tiles of `tile` CRUs (one of kTileSizes).  `opt` selects
+// the kernel variant that handles the per-cell build options of the lattice
+// update (perm, iso, slowncxchange, NCX form); without them a cell runs the
+// plain variant.
 template <class R>
-cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, int tile, cudaStream_t st);
+cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, bool opt, int tile,
+                        cudaStream_t st);
+
+// Whether a cell's lattice update uses any build option of the `opt` variant.
+inline bool cell_uses_options(const CellConst& c) {
+  return c.perm || c.iso || c.slowncx || c.ncx_form != RH_NCX_ALLOSTERIC;
+}
 
 template <class R>
 cudaError_t launch_init(const Lattice<R>& L, const CellConst* cells, const InitValues* iv,
