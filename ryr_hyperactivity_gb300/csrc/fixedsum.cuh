@@ -86,6 +86,41 @@ __device__ __forceinline__ void fx_warp_sum(uint64_t& lo, uint64_t& hi) {
   }
 }
 
+// Warp sum of one FP32 value per lane as value * 2^64 in 128-bit fixed
+// point, the same in every lane.  Cheaper than fx_from + fx_warp_sum: the
+// lanes align their 24-bit mantissas to the warp's largest exponent E
+// (value = m * 2^(e - 150), m scaled by 2^(34 - (E - e)), so 32 of them stay
+// below 2^63) and add them as 64-bit integers in a butterfly; only lanes
+// more than 2^34 below the warp's largest value lose low bits (an error
+// below 2^-58 of that value).  Integer adds, so the result does not depend
+// on the order of the lanes; `bad` as in fx_from.
+__device__ __forceinline__ void fx_warp_sum_f32(float v, uint64_t& lo, uint64_t& hi,
+                                                uint32_t& bad) {
+  const uint32_t b = __float_as_uint(v);
+  uint32_t e = (b >> 23) & 0xffu;
+  if (e >= 127u + kFxMaxExp) {  // also Inf and NaN; counted as 0
+    bad = 1u;
+    e = 0u;
+  }
+  const uint32_t E = __reduce_max_sync(0xffffffffu, e);
+  const uint32_t m = e ? ((b & 0x7fffffu) | 0x800000u) : 0u;  // zero and subnormals: 0
+  const int s = 34 - (int)(E - e);
+  int64_t x = s >= 0 ? (int64_t)((uint64_t)m << s) : (s > -32 ? (int64_t)(m >> -s) : 0);
+  if (b >> 31) x = -x;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+  // sum * 2^(E - 184) * 2^64 = x * 2^(E - 120), sh in [-120, 47]
+  const int sh = (int)E - 120;
+  const int64_t sx = x >> 63;  // sign fill
+  if (sh >= 0) {
+    lo = (uint64_t)x << sh;
+    hi = sh ? (uint64_t)(x >> (64 - sh)) : (uint64_t)sx;
+  } else {
+    lo = -sh < 64 ? (uint64_t)(x >> -sh) : (uint64_t)sx;
+    hi = (uint64_t)sx;
+  }
+}
+
 // Adds (lo, hi) to the 128-bit accumulator acc[0..1] (lo word first).
 __device__ __forceinline__ void fx_atomic_add(unsigned long long* acc, uint64_t lo, uint64_t hi) {
   const unsigned long long old = atomicAdd(acc, (unsigned long long)lo);

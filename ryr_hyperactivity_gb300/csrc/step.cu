@@ -910,10 +910,14 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
 #pragma unroll
     for (int qq = 0; qq < 3; ++qq) {
       uint64_t lo, hi;
-      fx_from(pv[qq], lo, hi, bad);
-      fx_warp_sum(lo, hi);
-      lo = __shfl_sync(0xffffffffu, lo, 0);
-      hi = __shfl_sync(0xffffffffu, hi, 0);
+      if constexpr (sizeof(R) == 4) {
+        fx_warp_sum_f32(pv[qq], lo, hi, bad);  // every lane holds the sum
+      } else {
+        fx_from(pv[qq], lo, hi, bad);
+        fx_warp_sum(lo, hi);
+        lo = __shfl_sync(0xffffffffu, lo, 0);
+        hi = __shfl_sync(0xffffffffu, hi, 0);
+      }
       if (lane == qq) {
         qlo = lo;
         qhi = hi;
