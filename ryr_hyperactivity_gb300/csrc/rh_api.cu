@@ -518,7 +518,9 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
     if (s->ts < 0) return fail(s, RH_ERR_ARG, "block_size %d is not a compiled tile length", want);
   }
   s->hcells = s->sets[s->ts].hcells;
-  if (off > INT32_MAX - 256) return fail(s, RH_ERR_ARG, "ensemble too large (%lld CRUs)", (long long)off);
+  // the step kernel indexes the arena with 32-bit element offsets (8 per CRU)
+  if (off > ((int64_t)1 << 29))
+    return fail(s, RH_ERR_ARG, "ensemble too large (%lld CRUs, at most 2^29)", (long long)off);
   s->stride = off;
   s->ls_rows_total = ls_off;
   s->device = s->opts.device;

@@ -38,11 +38,6 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-template <class R>
-__device__ __forceinline__ R clamp0(R x) {
-  return x < R(0) ? R(0) : x;
-}
-
 // ------------------------------------------------------------ cell update
 
 // Whole-cell part of the step, run by warp 0 (all 32 lanes) of the last CTA
@@ -219,13 +214,16 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   const int cell = tile.x;
   const int tid = threadIdx.x;
   const int cpad = (tile.z + 31) & ~31;  // cells are padded to 32 CRUs
-  const int64_t gt0 = (int64_t)(uint32_t)tile.w;  // arena index of the tile's first CRU
+  // Arena indices are 32-bit: the arena holds fewer than 2^29 CRUs (checked at
+  // creation), so every element index, 8 sub-voxels per CRU included, is
+  // below 2^32 and each address is one 32x64 multiply-add.
+  const uint32_t gt0 = (uint32_t)tile.w;  // arena index of the tile's first CRU
   if (kStage) {
     // Fields updated in place do not depend on the ping-pong parity, so
     // their copies start before the cell header arrives.  16-byte chunks:
     // a pair plane holds 2 CRUs per chunk, a 4-byte plane 4.
     const Lattice<R>& L = a.L;
-    const int64_t S = L.stride;
+    const uint32_t S = (uint32_t)L.stride;
     constexpr int kTpp = kBlock / 2;  // threads per pair plane
     const int c2 = tid % kTpp, h2 = tid / kTpp;
     if (TS::kStageBuf && 2 * c2 < cpad) {
@@ -293,14 +291,14 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   const bool out_step = OUT && sk.output_step && !a.lattice_only;
   const bool cadist_step = out_step && sk.cadist_step && a.out_cd != nullptr;
   const Lattice<R>& L = a.L;
-  const int64_t S = L.stride;
+  const uint32_t S = (uint32_t)L.stride;
   const int lx = sh.lx, ly = sh.ly, lz = sh.lz;
   const int lxly = lx * ly;
   const int count = tile.z;
   const int q = tile.y + tid;
   const bool valid = tid < count;
   const int par = sh.parity;
-  const int64_t g = sh.off + q;
+  const uint32_t g = (uint32_t)(sh.off + q);
   const V* ci2 = reinterpret_cast<const V*>(L.ci[par]);
   const V* cn2 = reinterpret_cast<const V*>(L.cnsr[par]);
 
@@ -474,7 +472,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     if (prevsp < 5 && nou + nob >= 5) nspark = 1;
     const R po = Math<R>::div(R(nou + nob), R(NRYR));
     R xire = R(0.0147 * SVJMAX) * po * (cjsr - cp) * R(1.0 / VP);
-    if (xire < R(0)) xire = R(0);
+    xire = clamp0(xire);
 
     // ---- NCX (:1296, subroutine_cuda.c:47-120); zero in a permeabilised
     //      cell, whose Ancx keeps its value (:1302) ----
@@ -557,7 +555,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         csn += dotcs * dth;
       }
     }
-    if (cp < R(0)) cp = R(0);
+    cp = clamp0(cp);
     if (csn < R(0)) csn = R(1e-6);
     cjsr = cjsr + dotcjsr * dt;
 
@@ -620,14 +618,14 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
 #pragma unroll 1
     for (int p = 0; p < 4; ++p) {
       const int by = p & 1, bx = p >> 1;
-      const int64_t gp = p * S + g;
+      const uint32_t gp = p * S + g;
       const V c = s_ci2[p][tid], n = s_cn2[p][tid];
       constexpr bool kSB = TS::kStageBuf;
       V catf = kSB ? s_buf[0][p][tid] : nb0, cats = kSB ? s_buf[1][p][tid] : nb1;
       V cacal = kSB ? s_buf[2][p][tid] : nb2, casr = kSB ? s_buf[3][p][tid] : nb3;
       V camyo = kSB ? s_buf[4][p][tid] : nb4, mgmyo = kSB ? s_buf[5][p][tid] : nb5;
       if (!kSB && p < 3) {
-        const int64_t gq = gp + S;
+        const uint32_t gq = gp + S;
         nb0 = catf2[gq], nb1 = cats2[gq], nb2 = cacal2[gq], nb3 = casr2[gq], nb4 = camyo2[gq];
         nb5 = mgmyo2[gq];
       }
@@ -870,7 +868,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         r[5] = (double)xire;
       }
       if (a.out_ls && y == sh.line_y && z == sh.line_z) {  // linescan row (:967-989), post-step values
-        const int64_t g0 = g;
+        const uint32_t g0 = g;
         double* r = a.out_ls + ((size_t)sh.ls_off + (size_t)sh.slot * lx + x) * RH_LINESCAN_COLS;
         r[0] = sh.t;
         r[1] = (double)(x + 1);
