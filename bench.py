@@ -247,13 +247,14 @@ def main():
                    "parallelism": f"cells sharded, {world} GPU(s)",
                    "tile_crus": tile, "cell_groups": sim.num_groups(),
                    "autotune_ms_per_step": {str(t): round(m, 4) for t, m in zip((64, 128, 256), tune_ms)}},
-        "gpu_launches": launches * sim.num_groups(),
+        "gpu_launches": 2 * launches * sim.num_groups(),  # lattice + cell update per group
         "timed_wall_s": wall,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if peak else None, "traffic": traffic,
                      "bytes_per_cru_update": bpc, "kernel_ms": avg_launch_s * 1e3,
-                     "kernel_ms_is": "one lattice update of every cell: one step-kernel launch per "
-                                     "cell group, the groups running concurrently",
+                     "kernel_ms_is": "one lattice update of every cell: per cell group one "
+                                     "step-kernel launch and one cell-update launch, the groups "
+                                     "running concurrently",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peak else None},
         "clocks": clk.summary(),
     }

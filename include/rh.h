@@ -145,7 +145,7 @@ typedef struct {
                                  output period) */
   int32_t cell_groups;        /* cells split into this many groups of about equal
                                  CRU count that advance on concurrent streams
-                                 (0 = 4; capped at the number of cells) */
+                                 (0 = 16; capped at the number of cells) */
   int32_t record_cadist;      /* 1 = keep cadist records (the reference's
                                  outputcadist build, :1001-1013): every 5 ms in the
                                  first 500 ms of each pacing period, t, V and 6
@@ -294,7 +294,8 @@ int rh_bytes_per_cru_step(const rh_sim* sim, double* bytes);
 /* Device time of the lattice updates, accumulated since the last call (CUDA
  * events on the simulator's stream around the work it enqueued); returns the
  * number of lattice updates (time steps) and milliseconds.  Each update is
- * one step-kernel launch per cell group (rh_num_groups). */
+ * two kernel launches per cell group (rh_num_groups): the lattice step and
+ * the cells' whole-cell update. */
 int rh_kernel_timing(rh_sim* sim, int64_t* launches, double* ms);
 
 /* Number of cell groups advanced on concurrent streams (run option

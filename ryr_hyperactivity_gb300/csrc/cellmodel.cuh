@@ -113,7 +113,10 @@ __host__ __device__ inline void membrane_update(rh_membrane& m, double dt, const
   m.xr = xkrinf - (xkrinf - m.xr) * exp(-dt / taukr);
   // IKs (:534-559)
   double prnak = 0.0183300;
-  double qks_inf = 0.2 * (1 + (c.slowncx ? 1.6 : 0.8) / (1 + pow((0.28 / csubt), 3.0)));
+  // pow((0.28 / csubt), 3) and, below, pow(12 / xnai, 1) of the reference are
+  // evaluated as the product and the quotient itself
+  const double q28 = 0.28 / csubt;
+  double qks_inf = 0.2 * (1 + (c.slowncx ? 1.6 : 0.8) / (1 + q28 * q28 * q28));
   double tauqks = c.slowncx ? 2000 : 1000.00;  // :540-543
   double eks = (1.00 / FRT) * log((xko + prnak * XNAO) / (xki + prnak * xnai));
   double xs1ss = 1.0 / (1.0 + exp(-(v - 1.500) / 16.700));
@@ -155,7 +158,7 @@ __host__ __device__ inline void membrane_update(rh_membrane& m, double dt, const
   // INaK (:665-676)
   double sigma = (exp(XNAO / 67.30) - 1.00) / 7.00;
   double fnak = 1.00 / (1.0 + 0.1245 * exp(-0.1 * v * FRT) + 0.0365 * sigma * exp(-v * FRT));
-  double xinak = 1. * 1.5000 * fnak * (1.0 / (1.0 + pow((12.00 / xnai), 1.00))) * xko / (xko + 1.50);
+  double xinak = 1. * 1.5000 * fnak * (1.0 / (1.0 + (12.00 / xnai))) * xko / (xko + 1.50);
   // stimulus (:689-692)
   double stim = stimulus(c, t, c.iso ? fmod(t, tperid) : fmod(t + tperid - 100, tperid));
   // [Na]i and V (:701-738)

@@ -4,12 +4,19 @@
 // FP64 runs at a small fraction of the FP32 rate on this GPU, and a warp
 // instruction costs the FP64 pipe the same time whether one lane or 32 lanes
 // are active.  The serial versions evaluate some 55 exponentials, 60
-// divisions, three logarithms, two powers and three fmods one after the other
-// in one lane; here every group of mutually independent transcendentals and
+// divisions, three logarithms and three fmods one after the other in one
+// lane; here every group of mutually independent transcendentals and
 // divisions is evaluated in one SIMT call, one operand set per lane, through
 // a 32-slot shared-memory exchange.  Each operation keeps its operands and
-// its order, so the results are bit-identical to the serial versions (which
-// the CPU oracle restates); only the lane that computes each value changes.
+// its order, so the results are bit-identical to the serial versions; only
+// the lane that computes each value changes.  The reference's two powers,
+// pow(0.28/csubt, 3) and pow(12/xnai, 1), are a product and the quotient
+// itself in both versions (the CPU oracle keeps pow; the results differ in
+// the last bits).
+//
+// The membrane step is split at the point where it needs the lattice sums:
+// membrane_pre_warp runs while the cell's lattice launch is still finishing,
+// membrane_post_warp after it.
 //
 // All 32 lanes of the calling warp must be active and call with identical
 // arguments; every lane returns the same results.
@@ -136,16 +143,32 @@ struct WarpSlots {
   __device__ __forceinline__ double get(int i) const { return r[i]; }
 };
 
-// Membrane step (membrane_update, cellmodel.cuh) by one warp.  `s` is 160
-// doubles of shared memory owned by the warp.  The lattice sums come in as
-// tot (sum cs, sum xicat, sum xinaca over the cell's CRUs, :447-456); the
-// function also computes the fmods of this step (stimulus phase and the next
-// lattice update's window flags: reset, output, the two cadist conditions
-// and the iso LCC phase) into fm[0..5].
-__device__ inline void membrane_update_warp(rh_membrane& m, double dt, const CellConst& c,
-                                            const double tot[3], double* s, double fm[6]) {
+// Results of the membrane step (membrane_update, cellmodel.cuh) that do not
+// depend on the step's lattice sums: the currents of the old state, the
+// stimulus and the two constants of the qks update.
+struct MembranePre {
+  double xina, xikr, xiks, xik1, xitos, xitof, xinak, stim;
+  double qks_num, tauqks;  // qks_inf = 0.2 (1 + qks_num / (1 + (0.28/csubt)^3))
+};
+
+// The qks update, which needs csubt and nothing downstream of the new
+// voltage; step_coef_warp evaluates it in spare slots of its own rounds.
+struct QksStep {
+  double csubt, qks, qks_num, tauqks;  // in
+  double dqks;                          // out: dt (qks_inf - qks) / tauqks
+};
+
+// Membrane step by one warp, first part: everything that needs only the
+// state of the previous step (:458-700 without the reduction), run before
+// the cell update waits for its lattice launch.  Gates are advanced in `m`;
+// m.qks, m.xnai, m.v and the reduction quotients are left to
+// membrane_post_warp.  `s` is 160 doubles of shared memory owned by the warp;
+// fm[0..5] receives the fmods of this step (stimulus phase and the next
+// lattice update's window flags: reset, output, the two cadist conditions and
+// the iso LCC phase).
+__device__ inline void membrane_pre_warp(rh_membrane& m, double dt, const CellConst& c, double* s,
+                                         double fm[6], MembranePre& P) {
   const double tperid = c.pcl, svikr = c.svikr;
-  const int nin = c.n;
   const int lane = threadIdx.x & 31;
   WarpSlots w{s, s + 32, s + 64, lane};
   const double t = m.t, v = m.v;
@@ -153,35 +176,19 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   const double xnai = m.xnai;
   const double prnak = 0.0183300;
 
-  // ---- round 0: reduction quotients, log and pow arguments ----
-  w.open(7);
+  // ---- round 0: log arguments and the INaK quotient ----
+  w.open(4);
   w.put(0, XNAO, xnai);                                  // ena
   w.put(1, xko, xki);                                    // ek
   w.put(2, xko + prnak * XNAO, xki + prnak * xnai);      // eks
-  w.put(3, 12.00, xnai);                                 // INaK pow base
-  w.put(4, tot[0], (double)nin);                         // csubt (:447)
-  w.put(5, tot[1], CM);                                  // xicatto (:452)
-  w.put(6, tot[2], CM);                                  // xinacato (:456)
+  w.put(3, 12.00, xnai);                                 // INaK base, 12/xnai
   w.divide();
-  const double csubt = w.get(4);
-  m.csubt = csubt;
-  m.xicatto = w.get(5) * 0.0965 * VP * 2.0 * (ICAGAMMA + 1.);
-  m.xinacato = w.get(6) * 0.0965 * VS;
   // logarithms (lanes 0-2)
   const double lgv = log(w.r[lane]);
   const double ena = (1.0 / FRT) * __shfl_sync(0xffffffffu, lgv, 0);
   const double ek = (1.00 / FRT) * __shfl_sync(0xffffffffu, lgv, 1);
   const double eks = (1.00 / FRT) * __shfl_sync(0xffffffffu, lgv, 2);
-  const double q12 = w.get(3);
-  // the IKs pow base needs csubt
-  w.open(1);
-  w.put(0, 0.28, csubt);
-  w.divide();
-  const double q28 = w.get(0);
-  // powers: lane 0 pow(0.28/csubt, 3), lane 1 pow(12/xnai, 1)
-  const double pw = pow(lane == 0 ? q28 : q12, lane == 0 ? 3.0 : 1.00);
-  const double pow_ks = __shfl_sync(0xffffffffu, pw, 0);
-  const double pow_nak = __shfl_sync(0xffffffffu, pw, 1);
+  const double pow_nak = w.get(3);  // pow(12/xnai, 1) = 12/xnai
   // fmods: stimulus phase (:689, iso :683) and the next update's window,
   // output, cadist and iso LCC flags (:1244, :777, :1002, :1213)
   {
@@ -219,7 +226,7 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   // ---- round 2: first-level divisions ----
   const double bm = 0.08 * E[1];
   double ah, bh, aj, bj, am;
-  w.open(20);
+  w.open(19);
   w.put(0, 0.32 * (v + 47.13), 1.0 - E[0]);                    // am
   if (low) {
     w.put(1, v + 37.78, 1.0 + E[7]);                           // aj factor
@@ -232,7 +239,7 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   w.put(4, 0.000610 * (v + 10.00), E[11] - 1.00);              // xkrv2
   w.put(5, 1.00, 1.00 + E[12]);                                // xkrinf
   w.put(6, 1.00, 1.00 + E[13]);                                // rg
-  w.put(7, c.slowncx ? 1.6 : 0.8, 1 + pow_ks);                 // qks_inf term (:537, :541)
+  w.put(7, 1.0, 1.0 + pow_nak);                                // INaK factor
   w.put(8, 1.0, 1.0 + E[14]);                                  // xs1ss
   w.put(9, 0.0000719 * (v + 30.00), 1.00 - E[15]);             // tauxs term 1
   w.put(10, 0.0001310 * (v + 30.00), E[16] - 1.00);            // tauxs term 2
@@ -244,7 +251,6 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   w.put(16, 3000.00, 1.0 + E[24]);                             // tys
   w.put(17, 20.0, 1.0 + E[22]);                                // tyf
   w.put(18, E[26] - 1.00, 7.00);                               // sigma
-  w.put(19, 1.0, 1.0 + pow_nak);                               // INaK factor
   w.divide();
   am = w.get(0);
   if (low) {
@@ -259,19 +265,17 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
     bj = w.get(2);
   }
   const double xkrv1 = w.get(3), xkrv2 = w.get(4), xkrinf = w.get(5), rg = w.get(6);
-  const double qks_inf = 0.2 * (1 + w.get(7));
+  const double nak_f = w.get(7);
   const double xs1ss = w.get(8);
   const double aki = w.get(11), bki = w.get(12);
   const double xtos_inf = w.get(13), ytos_inf = w.get(14), rs_inf = w.get(14);
   const double txs = w.get(15) + 0.50, tys = w.get(16) + 30.00;
   const double txf = 3.50 * E[25] + 1.50, tyf = w.get(17) + 20.00;
   const double sigma = w.get(18);
-  const double nak_f = w.get(19);
   const double tauxs_sum = w.get(9) + w.get(10);
 
   // ---- round 3: second-level divisions ----
-  const double tauqks = c.slowncx ? 2000 : 1000.00;  // :538, :542
-  w.open(11);
+  w.open(10);
   w.put(0, 1.00, ah + bh);                                     // tauh
   w.put(1, 1.00, aj + bj);                                     // tauj
   w.put(2, 1.00, am + bm);                                     // taum
@@ -282,13 +286,12 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   w.put(7, 1.00, tauxs_sum);                                   // tauxs
   w.put(8, aki, aki + bki);                                    // xkin
   w.put(9, 1.00, 1.0 + 0.1245 * E[27] + 0.0365 * sigma * E[28]);  // fnak
-  w.put(10, dt * (qks_inf - m.qks), tauqks);                   // qks increment
   w.divide();
   const double tauh = w.get(0), tauj = w.get(1), taum = w.get(2);
   const double rh_ = w.get(3), rj_ = w.get(4), rm_ = w.get(5);
   const double taukr = w.get(6);
   const double tauxs = 0.95 * w.get(7);
-  const double xkin = w.get(8), fnak = w.get(9), dqks = w.get(10);
+  const double xkin = w.get(8), fnak = w.get(9);
 
   // ---- round 4: gate exponent arguments and INaK ----
   w.open(10);
@@ -303,7 +306,7 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
   w.put(8, -dt, tyf);
   w.put(9, 1. * 1.5000 * fnak * nak_f * xko, xko + 1.50);      // xinak
   w.divide();
-  const double xinak = w.get(9);
+  P.xinak = w.get(9);
   double* const G = s + 128;  // exp(-dt/tau) of the nine gates
   {
     const double ge = exp(lane < 9 ? w.r[lane] : 0.0);
@@ -311,50 +314,72 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
     __syncwarp();
   }
 
-  // ---- serial remainder (identical in every lane) ----
+  // ---- currents of the old state and the gate updates (identical in
+  //      every lane) ----
   const double gna = 15;
   const double gnaleak = 0.3e-3 * 5;
-  const double xina = gna * m.xh * m.xj * m.xm * m.xm * m.xm * (v - ena) + gnaleak * (v - ena);
+  P.xina = gna * m.xh * m.xj * m.xm * m.xm * m.xm * (v - ena) + gnaleak * (v - ena);
   m.xh = rh_ - (rh_ - m.xh) * G[0];
   m.xj = rj_ - (rj_ - m.xj) * G[1];
   m.xm = rm_ - (rm_ - m.xm) * G[2];
   const double gss = sqrt(xko / 5.40);
   const double gkr = 0.0078360;
-  const double xikr = svikr * gkr * gss * m.xr * rg * (v - ek);
+  P.xikr = svikr * gkr * gss * m.xr * rg * (v - ek);
   m.xr = xkrinf - (xkrinf - m.xr) * G[3];
   const double gksx = 0.2000;
-  const double xiks = 1.0 * 1. * gksx * m.qks * m.xs1 * m.xs2 * (v - eks);
+  P.xiks = 1.0 * 1. * gksx * m.qks * m.xs1 * m.xs2 * (v - eks);
   m.xs1 = xs1ss - (xs1ss - m.xs1) * G[4];
   m.xs2 = xs1ss - (xs1ss - m.xs2) * G[4];
-  m.qks = m.qks + dqks;
+  P.qks_num = c.slowncx ? 1.6 : 0.8;         // :537, :541
+  P.tauqks = c.slowncx ? 2000 : 1000.00;     // :538, :542
   const double gki = 0.600 * (sqrt(xko / 5.4));
-  const double xik1 = (1.0) * gki * xkin * (v - ek);
-  const double xitos = 1.0 * 0.040 * m.xtos * (m.ytos + 0.50 * rs_inf) * (v - ek);
+  P.xik1 = (1.0) * gki * xkin * (v - ek);
+  P.xitos = 1.0 * 0.040 * m.xtos * (m.ytos + 0.50 * rs_inf) * (v - ek);
   m.xtos = xtos_inf - (xtos_inf - m.xtos) * G[5];
   m.ytos = ytos_inf - (ytos_inf - m.ytos) * G[6];
-  const double xitof = 1.0 * 0.10 * m.xtof * m.ytof * (v - ek);
+  P.xitof = 1.0 * 0.10 * m.xtof * m.ytof * (v - ek);
   m.xtof = xtos_inf - (xtos_inf - m.xtof) * G[7];
   m.ytof = ytos_inf - (ytos_inf - m.ytof) * G[8];
-  const double stim = stimulus(c, t, fm[0]);
+  P.stim = stimulus(c, t, fm[0]);
+}
+
+// Membrane step by one warp, second part, once the lattice sums tot (sum cs,
+// sum xicat, sum xinaca over the cell's CRUs, :447-456) are in: the
+// reduction quotients, [Na]i and V (:701-738), and the currents into `m`.
+// m.t and m.v still hold the old step's time and voltage.
+__device__ inline void membrane_post_warp(rh_membrane& m, double dt, const CellConst& c,
+                                          const double tot[3], double* s, const MembranePre& P) {
+  const int lane = threadIdx.x & 31;
+  WarpSlots w{s, s + 32, s + 64, lane};
+  const double t = m.t, v = m.v;
+  const double xnai = m.xnai;
+  w.open(3);
+  w.put(0, tot[0], (double)c.n);                         // csubt (:447)
+  w.put(1, tot[1], CM);                                  // xicatto (:452)
+  w.put(2, tot[2], CM);                                  // xinacato (:456)
+  w.divide();
+  m.csubt = w.get(0);
+  m.xicatto = w.get(1) * 0.0965 * VP * 2.0 * (ICAGAMMA + 1.);
+  m.xinacato = w.get(2) * 0.0965 * VS;
   const double wcainv = 1.0 / 50.0;
   const double conv = 0.18 * 12500;
   const double xrr = 1.0 * (1.0 / wcainv / conv) / 1000.0;
-  const double dnai = -xrr * (xina + 3.0 * xinak + 3.0 * m.xinacato);
+  const double dnai = -xrr * (P.xina + 3.0 * P.xinak + 3.0 * m.xinacato);
   m.xnai = xnai + dnai * dt;
-  const double dvh = -(xina + xik1 + 1 * xikr + 1 * xiks + xitos + 1 * xitof + 1. * m.xinacato +
-                       1 * m.xicatto + xinak) +
-                     stim;
+  const double dvh = -(P.xina + P.xik1 + 1 * P.xikr + 1 * P.xiks + P.xitos + 1 * P.xitof +
+                       1. * m.xinacato + 1 * m.xicatto + P.xinak) +
+                     P.stim;
   m.v = protocol_voltage(c, t, dt, v + dvh * dt);
   m.out_ica += m.xicatto;
   m.out_ncx += m.xinacato;
-  m.out_ina += xina;
-  m.xina = xina;
-  m.xiks = xiks;
-  m.xikr = xikr;
-  m.xik1 = xik1;
-  m.xinak = xinak;
-  m.xitos = xitos;
-  m.xitof = xitof;
+  m.out_ina += P.xina;
+  m.xina = P.xina;
+  m.xiks = P.xiks;
+  m.xikr = P.xikr;
+  m.xik1 = P.xik1;
+  m.xinak = P.xinak;
+  m.xitos = P.xitos;
+  m.xitof = P.xitof;
 }
 
 // Coefficients of the next lattice update (step_coef, cellmodel.cuh) by one
@@ -364,7 +389,7 @@ __device__ inline void membrane_update_warp(rh_membrane& m, double dt, const Cel
 // memory owned by the warp.  Returns whether the cell is inside its protocol.
 __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
                                       const CellConst& c, double dt, const double* fm,
-                                      double* s) {
+                                      double* s, QksStep* qs = nullptr) {
   const double fm1 = fm[0], fm2 = fm[1];
   const int lane = threadIdx.x & 31;
   WarpSlots w{s, s + 32, s + 64, lane};
@@ -379,7 +404,7 @@ __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
     fvk = 8.5;
   }
   // ---- round 1: quotients that do not need za ----
-  w.open(8);
+  w.open(qs ? 9 : 8);
   w.put(0, v * FARAD, XRGAS);                  // za, first division
   w.put(1, xnai, KMNAI);                       // r
   w.put(2, 1.0, dt);                           // rdt
@@ -388,6 +413,7 @@ __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
   w.put(5, -(v - dv5), dvk);                   // dinf / taudin exponent
   w.put(6, -(v - fv5), fvk);                   // finf exponent 1
   w.put(7, (v - 60), 12.);                     // finf exponent 2
+  if (qs) w.put(8, 0.28, qs->csubt);           // qks: 0.28/csubt
   w.divide();
   const double za1 = w.get(0), r = w.get(1);
   k.rdt = w.get(2);
@@ -395,12 +421,17 @@ __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
   k.rdt95 = w.get(4);
   const double x_d = w.get(5), x_f1 = w.get(6), x_f2 = w.get(7);
   // ---- round 2: za, rdth95 ----
-  w.open(2);
+  double q28 = 0.0;
+  if (qs) q28 = w.get(8);
+  w.open(qs ? 3 : 2);
   w.put(0, za1, TEMPER);
   w.put(1, 0.95, k.dth);
+  if (qs) w.put(2, qs->qks_num, 1 + q28 * q28 * q28);  // pow(0.28/csubt, 3) as a product
   w.divide();
   const double za = w.get(0);
   k.rdth95 = w.get(1);
+  double qks_inf = 0.0;
+  if (qs) qks_inf = 0.2 * (1 + w.get(2));
   // ---- round 3: exponentials ----
   const double tq = 0.0337 * (v + 10.5);
   double X[7];
@@ -420,13 +451,15 @@ __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
   const double e2z = X[4], e1 = X[5], e2 = X[6];
   const bool za_small = fabs(za) < 0.001;
   // ---- round 4 ----
-  w.open(5);
+  w.open(qs ? 6 : 5);
   w.put(0, 1.0, 1.0 + X[0]);                                   // dinf
   w.put(1, 1.0, 1.0 + X[1]);                                   // finf term
   w.put(2, 1.0 - X[0], 0.035 * (v - dv5));                     // taudin inner
   w.put(3, 4.0 * PCA * za * FARAD * GAMMAI, e2z - 1.0);        // lcc_k
   w.put(4, e2z, 1000.0);                                       // lcc_e2z_k
+  if (qs) w.put(5, dt * (qks_inf - qs->qks), qs->tauqks);  // qks increment
   w.divide();
+  if (qs) qs->dqks = w.get(5);
   const double dinf = w.get(0);
   const double f_a = w.get(1), td_in = w.get(2);
   k.lcc_k = za_small ? 2.0 * PCA * FARAD * GAMMAI : w.get(3);

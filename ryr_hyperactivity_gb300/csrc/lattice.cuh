@@ -87,14 +87,14 @@ struct CellDyn {
   uint32_t status;
   int parity;
   int done;
-  unsigned int arrive;  // warps of this cell that finished the current step
+  unsigned int arrive;  // reserved, always 0 (kept for the exported state layout)
   long long out_count;  // output records produced
   BeatTracker bt;       // per-beat statistics in progress
   long long stats_count;  // beat records produced
   long long cd_count;     // cadist records produced
   // sum cs, xicat, xinaca of the step in progress as 128-bit fixed point
-  // (value * 2^64, lo word first), added to by every CTA of the cell and
-  // read and cleared by the last one (fixedsum.cuh)
+  // (value * 2^64, lo word first), added to by every warp of the cell's
+  // lattice CTAs, read and cleared by the cell's update (fixedsum.cuh)
   unsigned long long acc[6];
 };
 

@@ -232,22 +232,28 @@ StepArgs<R> make_args(rh_sim* s, const Lattice<R>& L, bool lattice_only) {
   return a;
 }
 
-// One group's step: the tiles of cells [group_cell[g], group_cell[g+1]).
+// One group's step: the tiles of cells [group_cell[g], group_cell[g+1]),
+// then the whole-cell update of those cells.
 cudaError_t launch_group(rh_sim* s, int g, bool out, bool lattice_only, cudaStream_t st) {
   const rh_sim::TileSet& t = s->sets[s->ts];
-  const int tb = t.hcells[s->group_cell[g]].tile_begin;
-  const int te = s->group_cell[g + 1] < s->ncells ? t.hcells[s->group_cell[g + 1]].tile_begin
-                                                  : t.ntiles;
+  const int c0 = s->group_cell[g], c1 = s->group_cell[g + 1];
+  const int tb = t.hcells[c0].tile_begin;
+  const int te = c1 < s->ncells ? t.hcells[c1].tile_begin : t.ntiles;
+  cudaError_t e;
   if (is_mixed(s)) {
     StepArgs<float> a = make_args(s, s->Lf, lattice_only);
     a.tiles += tb;
     a.tile_base = tb;
-    return launch_step<float>(a, te - tb, out, s->group_opt[g], t.tile, st);
+    if ((e = launch_step<float>(a, te - tb, out, s->group_opt[g], t.tile, st)) != cudaSuccess)
+      return e;
+    return launch_cells<float>(a, c0, c1 - c0, out, t.tile, st);
   }
   StepArgs<double> a = make_args(s, s->Ld, lattice_only);
   a.tiles += tb;
   a.tile_base = tb;
-  return launch_step<double>(a, te - tb, out, s->group_opt[g], t.tile, st);
+  if ((e = launch_step<double>(a, te - tb, out, s->group_opt[g], t.tile, st)) != cudaSuccess)
+    return e;
+  return launch_cells<double>(a, c0, c1 - c0, out, t.tile, st);
 }
 
 // `n` steps of every group: group g's launches go to its own stream, forked

@@ -1,7 +1,8 @@
-// step.cu — the fused per-time-step kernel.
+// step.cu — the per-time-step kernels.
 //
-// One launch advances every active cell by one time step:
-//   1. each CTA owns a tile of up to B consecutive CRUs of one cell and
+// Two launches per cell group advance every active cell of the group by one
+// time step, with no host round trip:
+//   1. step_kernel: each CTA owns a tile of up to B consecutive CRUs of one cell and
 //      updates them as the reference's Compute kernel does
 //      (cuda_Cell_Detailed.cu:1187-1692, fixA): the tile's own ci/cnsr
 //      sub-voxels are staged in shared memory so that in-tile stencil
@@ -10,13 +11,12 @@
 //   2. the CTA reduces sum(cs), sum(xicat), sum(xinaca) exactly in 128-bit
 //      fixed point (fixedsum.cuh) and adds them to the cell's accumulators
 //      with integer atomics; at output steps it also stores the ~30
-//      statistics of :839-929 as one FP64 partial per tile;
-//   3. the last CTA of a cell to finish (atomic arrival counter) reads the
+//      statistics of :839-929 as one FP64 partial row per warp;
+//   2. cell_kernel, next on the same stream: one warp per cell reads the
 //      sums (and sums the output partials in a fixed order), runs the
-//      membrane model and V update (:430-739, the reference's host loop)
-//      with one warp, writes the output record at output steps, and
-//      prepares the coefficients of the next step.
-// A time step is therefore one kernel launch with no host round trip.
+//      membrane model and V update (:430-739, the reference's host loop),
+//      writes the output record at output steps, and prepares the
+//      coefficients of the next step.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -38,95 +38,142 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// ------------------------------------------------------- launch ordering
+
+// Programmatic dependent launch: the cell update of a group is launched with
+// programmatic stream serialization after the group's lattice launch, so its
+// CTAs may start once every lattice CTA has started (each signals at entry).
+// It does the part of the membrane step that needs only the previous step's
+// state, then waits in griddepcontrol.wait until the lattice launch has
+// completed and its memory is visible.  Without the launch attribute the wait
+// returns at once.
+__device__ __forceinline__ void allow_dependent_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void wait_for_prerequisite_grid() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // ------------------------------------------------------------ cell update
 
-// Whole-cell part of the step, run by warp 0 (all 32 lanes) of the last CTA
-// of the cell.  `scratch` is 160 doubles of shared memory no longer used by
-// the tile.  Not inlined: its FP64 working set would otherwise shape the
-// register allocation of the lattice code, which runs on every CTA.
-template <class R>
-__noinline__ __device__ void cell_update(const StepArgs<R>& a, int cell, bool out_step, double* scratch,
-                                         int nw, bool cadist) {
+// Whole-cell part of the step for cells [cell0, cell0 + gridDim.x): one warp
+// per cell, launched on the group's stream right after the group's lattice
+// launch.  Before the wait it reads only what the previous step's cell
+// update wrote (that launch completed before the lattice launch began): the
+// membrane state, the flags of the step just taken, the cell constants.
+// After the wait: the exact lattice sums, the output partials, the status
+// bits the lattice CTAs set.  Then V and [Na]i (:430-739, the reference's
+// host loop), the coefficients of the next step, the output record and the
+// per-beat statistics.  A separate launch keeps this FP64 work (tens of
+// microseconds of dependent FP64 latency on this GPU) out of the lattice
+// CTAs; at <= 128 registers a cell warp fits beside five lattice CTAs.
+// `nw` is the number of warps per lattice tile (the rows of output partials
+// each tile wrote).
+template <class R, bool OUT>
+__global__ void __launch_bounds__(32, 16) cell_kernel(StepArgs<R> a, int cell0, int nw) {
+  __shared__ double scratch[160];
   const int lane = threadIdx.x & 31;
+  const int cell = cell0 + blockIdx.x;
   CellDyn* dyn = a.dyn + cell;
+  if (dyn->done) return;  // its lattice CTAs returned at once as well
+  // the flags of the step just taken, read before the update replaces them
+  const StepCoef<R>* kc = coef_ptr<R>(dyn);
+  const bool out_step = OUT && kc->output_step && !a.lattice_only;
+  const bool cadist = out_step && kc->cadist_step && a.out_cd != nullptr;
   const CellConst& cc = a.cells[cell];
-  const double* P = a.partials;
-  // output-step partials: one row per warp of each of the cell's tiles
-  const int t0 = cc.tile_begin * nw, nt = cc.tile_count * nw;
-  // the step's exact whole-cell sums, accumulated by the cell's CTAs
-  double tot[3];
-#pragma unroll
-  for (int q = 0; q < 3; ++q)
-    tot[q] = fx_to_double(__ldcg(&dyn->acc[2 * q]), __ldcg(&dyn->acc[2 * q + 1]));
-  double osum[NOUT];
-  if (out_step) {
-    for (int q = 0; q < NOUT; ++q) {
-      double s = 0.0;
-      for (int tl = lane; tl < nt; tl += 32)
-        s += __ldcg(P + (size_t)(t0 + tl) * P_COUNT + P_STEP_END + q);
-      osum[q] = warp_sum(s);
-    }
-    // the ci > 1000 flag is a max, not a sum
-    double f = 0.0;
-    for (int tl = lane; tl < nt; tl += 32)
-      f = fmax(f, __ldcg(P + (size_t)(t0 + tl) * P_COUNT + O_CIHIGH));
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) f = fmax(f, __shfl_down_sync(0xffffffffu, f, off));
-    osum[O_CIHIGH - P_STEP_END] = f;
-  }
-  rh_membrane m = dyn->m;
   const double dt = a.dt;
-  // reduction (:447-456) and membrane model (:458-739), warp-parallel
+  rh_membrane m = dyn->m;
+  MembranePre pre;
   double fm[6];
-  membrane_update_warp(m, dt, cc, tot, scratch, fm);
-  uint32_t status = dyn->status;
-  if (!isfinite(m.v) || !isfinite(m.xnai) || !isfinite(m.csubt) || !isfinite(m.xicatto) ||
-      !isfinite(m.xinacato))
-    status |= RH_STATUS_NAN;
-  if (lane == 0) {
-    if (a.stats) {  // per-beat detectors on the (t, V) sample of this step
-      rh_beat_stats rec;
-      if (beat_on_step(dyn->bt, m.t, m.v, cc.pcl, &rec)) {
-        a.stats[(size_t)cell * a.stats_cap + dyn->stats_count % a.stats_cap] = rec;
-        dyn->stats_count += 1;
-      }
-    }
+  if (!a.lattice_only) membrane_pre_warp(m, dt, cc, scratch, fm, pre);
+
+  wait_for_prerequisite_grid();
+
+  if (!a.lattice_only) {
+    const double* P = a.partials;
+    // output-step partials: one row per warp of each of the cell's tiles
+    const int t0 = cc.tile_begin * nw, nt = cc.tile_count * nw;
+    // the step's exact whole-cell sums, accumulated by the cell's CTAs
+    double tot[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      tot[q] = fx_to_double(__ldcg(&dyn->acc[2 * q]), __ldcg(&dyn->acc[2 * q + 1]));
+    double osum[NOUT];
     if (out_step) {
-      m.sparksum += (long long)osum[O_SPARK - P_STEP_END];
-      if (osum[O_CIHIGH - P_STEP_END] > 0) status |= RH_STATUS_CI_HIGH;
-      long long slot = dyn->out_count % a.out_cap;
-      double* w = a.out_wc + ((size_t)cell * a.out_cap + slot) * RH_WHOLECELL_COLS;
-      wholecell_columns(w, osum, m, cc.n, dt);
-      if (cadist && a.out_cd) {  // record header: t and V of this output step (:1005)
-        double* h = a.out_cd + cc.cd_off + (dyn->cd_count % a.cd_cap) * (2 + 6 * (long long)cc.n);
-        h[0] = m.t;
-        h[1] = m.v;
-        dyn->cd_count += 1;
+      for (int q = 0; q < NOUT; ++q) {
+        double s = 0.0;
+        for (int tl = lane; tl < nt; tl += 32)
+          s += __ldcg(P + (size_t)(t0 + tl) * P_COUNT + P_STEP_END + q);
+        osum[q] = warp_sum(s);
       }
-      if (a.stats) beat_on_output(dyn->bt, w);
-      dyn->out_count += 1;
-      m.sparksum = 0;  // :1074-1077
-      m.out_ica = 0;
-      m.out_ncx = 0;
-      m.out_ina = 0;
+      // the ci > 1000 flag is a max, not a sum
+      double f = 0.0;
+      for (int tl = lane; tl < nt; tl += 32)
+        f = fmax(f, __ldcg(P + (size_t)(t0 + tl) * P_COUNT + O_CIHIGH));
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) f = fmax(f, __shfl_down_sync(0xffffffffu, f, off));
+      osum[O_CIHIGH - P_STEP_END] = f;
+    }
+    // reduction quotients, [Na]i and V (:447-456, :701-738)
+    membrane_post_warp(m, dt, cc, tot, scratch, pre);
+    uint32_t status = __ldcg(&dyn->status);
+    if (!isfinite(m.v) || !isfinite(m.xnai) || !isfinite(m.csubt) || !isfinite(m.xicatto) ||
+        !isfinite(m.xinacato))
+      status |= RH_STATUS_NAN;
+    const double t_step = m.t;  // the time the output record and statistics carry
+    m.t = m.t + dt;             // :1083
+    m.step += 1;
+    // coefficients of the next lattice update, with the qks update in spare
+    // slots of its rounds
+    StepCoef<double> kd;
+    QksStep qs{m.csubt, m.qks, pre.qks_num, pre.tauqks, 0.0};
+    const bool active = step_coef_warp(kd, m, cc, dt, fm + 1, scratch, &qs);
+    m.qks = m.qks + qs.dqks;
+    if (lane == 0) {
+      if (a.stats) {  // per-beat detectors on the (t, V) sample of this step
+        rh_beat_stats rec;
+        if (beat_on_step(dyn->bt, t_step, m.v, cc.pcl, &rec)) {
+          a.stats[(size_t)cell * a.stats_cap + dyn->stats_count % a.stats_cap] = rec;
+          dyn->stats_count += 1;
+        }
+      }
+      if (out_step) {
+        m.sparksum += (long long)osum[O_SPARK - P_STEP_END];
+        if (osum[O_CIHIGH - P_STEP_END] > 0) status |= RH_STATUS_CI_HIGH;
+        long long slot = dyn->out_count % a.out_cap;
+        double* w = a.out_wc + ((size_t)cell * a.out_cap + slot) * RH_WHOLECELL_COLS;
+        const double t_next = m.t;
+        m.t = t_step;
+        wholecell_columns(w, osum, m, cc.n, dt);
+        m.t = t_next;
+        if (cadist) {  // record header: t and V of this output step (:1005)
+          double* h = a.out_cd + cc.cd_off + (dyn->cd_count % a.cd_cap) * (2 + 6 * (long long)cc.n);
+          h[0] = t_step;
+          h[1] = m.v;
+          dyn->cd_count += 1;
+        }
+        if (a.stats) beat_on_output(dyn->bt, w);
+        dyn->out_count += 1;
+        m.sparksum = 0;  // :1074-1077
+        m.out_ica = 0;
+        m.out_ncx = 0;
+        m.out_ina = 0;
+      }
+      StepCoef<float> kf;
+      convert_coef(kf, kd);
+      if (!active) {
+        dyn->done = 1;
+        status |= RH_STATUS_DONE;
+      }
+      dyn->m = m;
+      dyn->cd = kd;
+      dyn->cf = kf;
+      dyn->status = status;
     }
   }
-  m.t = m.t + dt;  // :1083
-  m.step += 1;
-  StepCoef<double> kd;
-  const bool active = step_coef_warp(kd, m, cc, dt, fm + 1, scratch);
-  if (lane == 0) {
-    StepCoef<float> kf;
-    convert_coef(kf, kd);
-    if (!active) {
-      dyn->done = 1;
-      status |= RH_STATUS_DONE;
-    }
-    dyn->m = m;
-    dyn->cd = kd;
-    dyn->cf = kf;
-    dyn->status = status;
-  }
+  __syncwarp();
+  if (lane < 6) dyn->acc[lane] = 0ull;  // the next step starts from zero
+  if (lane == 0) dyn->parity ^= 1;
 }
 
 // ------------------------------------------------------------- step kernel
@@ -206,10 +253,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   R(*s_hz)[4][2][kBlock] = reinterpret_cast<R(*)[4][2][kBlock]>(dsm + TS::kHz);
   R(*s_hcs)[kBlock] = reinterpret_cast<R(*)[kBlock]>(dsm + TS::kHcs);
   V(*s_hx)[4][2] = reinterpret_cast<V(*)[4][2]>(dsm + TS::kHx);
-  // scratch of the cell update (run by the cell's last warp while other
-  // warps of the CTA may still be using the tile)
-  __shared__ double s_cu[160];
 
+  allow_dependent_launch();  // the cell update may start its first part
   const int4 tile = a.tiles[blockIdx.x];
   const int cell = tile.x;
   const int tid = threadIdx.x;
@@ -896,9 +941,9 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     }
   }
 
-  // ---- per-warp reduction and arrival: the per-step sums exactly
-  //      (fixedsum.cuh) into the cell's accumulators, the output-step
-  //      statistics as one FP64 partial row per warp; no CTA barrier ----
+  // ---- per-warp reduction: the per-step sums exactly (fixedsum.cuh) into
+  //      the cell's accumulators, the output-step statistics as one FP64
+  //      partial row per warp; no CTA barrier ----
   const int warp = tid >> 5, lane = tid & 31;
   constexpr int NW = kBlock / 32;
   uint64_t qlo = 0, qhi = 0;  // lane q < 3: the warp's sum q
@@ -940,23 +985,6 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   if (lane < 3) {
     fx_atomic_add(&a.dyn[cell].acc[2 * lane], qlo, qhi);
     if (lane == 0 && wst) atomicOr(&a.dyn[cell].status, wst);
-    __threadfence();  // the adds (and the output partials) before the arrival
-  }
-  __syncwarp();
-  int last = 0;
-  if (lane == 0) {
-    const unsigned int prev = atomicAdd(&a.dyn[cell].arrive, 1u);
-    last = prev == (unsigned)(sh.tile_count * NW - 1);
-  }
-  if (!__shfl_sync(0xffffffffu, last, 0)) return;
-  // ---- last warp of the cell: whole-cell update ----
-  __threadfence();
-  if (!a.lattice_only) cell_update<R>(a, cell, out_step, s_cu, NW, cadist_step);
-  __syncwarp();
-  if (lane < 6) a.dyn[cell].acc[lane] = 0ull;  // the next step starts from zero
-  if (lane == 0) {
-    a.dyn[cell].parity = par ^ 1;
-    a.dyn[cell].arrive = 0;
   }
 }
 
@@ -1085,6 +1113,34 @@ cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, bool opt, in
 }
 
 template <class R>
+cudaError_t launch_cells(const StepArgs<R>& a, int cell0, int ncells, bool out, int tile,
+                         cudaStream_t st) {
+  if (ncells <= 0) return cudaSuccess;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ncells);
+  cfg.blockDim = dim3(32);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  // Programmatic serialization after the lattice launch, and the device's
+  // highest launch priority: when lattice CTAs of the other groups are also
+  // waiting for an SM, the cell warps go first (measured: without the
+  // priority the early launch made the step slower).
+  int prio_low = 0, prio_high = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  at[1].id = cudaLaunchAttributePriority;
+  at[1].val.priority = prio_high;
+  cfg.attrs = at;
+  cfg.numAttrs = 2;
+  const int nw = tile / 32;
+  if (out) return cudaLaunchKernelEx(&cfg, cell_kernel<R, true>, a, cell0, nw);
+  return cudaLaunchKernelEx(&cfg, cell_kernel<R, false>, a, cell0, nw);
+}
+
+template <class R>
 cudaError_t launch_init(const Lattice<R>& L, const CellConst* cells, const InitValues* iv,
                         int ncells, int max_n, cudaStream_t st) {
   dim3 grid((max_n + 255) / 256, ncells);
@@ -1103,6 +1159,10 @@ template cudaError_t launch_step<double>(const StepArgs<double>&, int, bool, boo
                                          cudaStream_t);
 template cudaError_t launch_step<float>(const StepArgs<float>&, int, bool, bool, int,
                                         cudaStream_t);
+template cudaError_t launch_cells<double>(const StepArgs<double>&, int, int, bool, int,
+                                          cudaStream_t);
+template cudaError_t launch_cells<float>(const StepArgs<float>&, int, int, bool, int,
+                                         cudaStream_t);
 template cudaError_t launch_init<double>(const Lattice<double>&, const CellConst*,
                                          const InitValues*, int, int, cudaStream_t);
 template cudaError_t launch_init<float>(const Lattice<float>&, const CellConst*,
