@@ -149,6 +149,8 @@ struct WarpSlots {
 struct MembranePre {
   double xina, xikr, xiks, xik1, xitos, xitof, xinak, stim;
   double qks_num, tauqks;  // qks_inf = 0.2 (1 + qks_num / (1 + (0.28/csubt)^3))
+  // the time-step constants of StepCoef: 1/dt, dt/5, 0.95/dt, 0.95/(dt/5)
+  double rdt, dth, rdt95, rdth95;
 };
 
 // The qks update, which needs csubt and nothing downstream of the new
@@ -177,12 +179,18 @@ __device__ inline void membrane_pre_warp(rh_membrane& m, double dt, const CellCo
   const double prnak = 0.0183300;
 
   // ---- round 0: log arguments and the INaK quotient ----
-  w.open(4);
+  w.open(7);
   w.put(0, XNAO, xnai);                                  // ena
   w.put(1, xko, xki);                                    // ek
   w.put(2, xko + prnak * XNAO, xki + prnak * xnai);      // eks
   w.put(3, 12.00, xnai);                                 // INaK base, 12/xnai
+  w.put(4, 1.0, dt);                                     // rdt
+  w.put(5, dt, 5.0);                                     // dth
+  w.put(6, 0.95, dt);                                    // rdt95
   w.divide();
+  P.rdt = w.get(4);
+  P.dth = w.get(5);
+  P.rdt95 = w.get(6);
   // logarithms (lanes 0-2)
   const double lgv = log(w.r[lane]);
   const double ena = (1.0 / FRT) * __shfl_sync(0xffffffffu, lgv, 0);
@@ -226,7 +234,7 @@ __device__ inline void membrane_pre_warp(rh_membrane& m, double dt, const CellCo
   // ---- round 2: first-level divisions ----
   const double bm = 0.08 * E[1];
   double ah, bh, aj, bj, am;
-  w.open(19);
+  w.open(20);
   w.put(0, 0.32 * (v + 47.13), 1.0 - E[0]);                    // am
   if (low) {
     w.put(1, v + 37.78, 1.0 + E[7]);                           // aj factor
@@ -251,7 +259,9 @@ __device__ inline void membrane_pre_warp(rh_membrane& m, double dt, const CellCo
   w.put(16, 3000.00, 1.0 + E[24]);                             // tys
   w.put(17, 20.0, 1.0 + E[22]);                                // tyf
   w.put(18, E[26] - 1.00, 7.00);                               // sigma
+  w.put(19, 0.95, P.dth);                                      // rdth95
   w.divide();
+  P.rdth95 = w.get(19);
   am = w.get(0);
   if (low) {
     ah = 0.135 * E[2];
@@ -495,6 +505,118 @@ __device__ inline bool step_coef_warp(StepCoef<double>& k, const rh_membrane& m,
   k.dt = dt;
   k.reset_window = fm1 < dt;
   k.output_step = fm2 < dt;
+  k.perm = c.perm;
+  k.cadist_step = k.output_step && fm[2] < dt && fm[3] < 500;
+  return t < c.tend;
+}
+
+// The qks update of the mixed path in one division: with c3 = csubt^3 and
+// K = 0.28^3, qks_inf = 0.2 (c3 + K + num c3) / (c3 + K), so
+//   dqks = dt (0.2 (c3 + K + num c3) - qks (c3 + K)) / ((c3 + K) tauqks),
+// the reference's three quotients (q28, qks_inf, the increment) folded into
+// one (equal in exact arithmetic; the last bits differ).  `s` as in
+// membrane_post_warp; all lanes return the increment.
+__device__ inline double qks_increment_warp(double csubt, double qks, double num, double tauqks,
+                                            double dt, double* s) {
+  const int lane = threadIdx.x & 31;
+  WarpSlots w{s, s + 32, s + 64, lane};
+  constexpr double K = 0.28 * 0.28 * 0.28;
+  const double c3 = csubt * csubt * csubt;
+  const double d = c3 + K;
+  w.open(1);
+  w.put(0, dt * (0.2 * (d + num * c3) - qks * d), d * tauqks);
+  w.divide();
+  return w.get(0);
+}
+
+// Coefficients of the next lattice update for the FP32 lattice, computed in
+// FP32 from the FP64 membrane state (step_coef, cellmodel.cuh, restated): the
+// gating rates and the LCC/NCX factors are FP32 quantities of the mixed
+// path, and FP32 arithmetic keeps them off the long FP64 latency chain of the
+// cell update.  Where the FP64 form subtracts nearly equal values, the FP32
+// form avoids it: 1 - exp(x) and exp(2 za) - 1 as -expm1(x) and expm1(2 za),
+// 1 - dinf as exp(x) dinf, 1 - finf as the quotient it subtracts.  The flags
+// come from the FP64 fmods in fm (as step_coef_warp takes them) and the time
+// step constants from P.  Every lane returns the same coefficients.
+__device__ inline bool step_coef_warp_f32(StepCoef<float>& k, const rh_membrane& m,
+                                          const CellConst& c, double dt, const double* fm,
+                                          const MembranePre& P) {
+  const int lane = threadIdx.x & 31;
+  const double vd = m.v;
+  const float v = (float)vd, xnai = (float)m.xnai;
+  float dv5 = 5.f, dvk = 8.f, fv5 = -22.8f, fvk = 9.1f;
+  k.alphac = 0.22f;
+  k.betac = 4.f;
+  if (c.iso2) {
+    k.betac = 2.f;
+    dv5 = 0.f;
+    fv5 = -28.f;
+    fvk = 8.5f;
+  }
+  const float za = v * (float)(FARAD / XRGAS / TEMPER);
+  const float tq = 0.0337f * (v + 10.5f);
+  // one exponential per lane: lanes 0-6 the arguments of step_coef
+  const float arg = lane == 0 ? -(v - dv5) / dvk
+                  : lane == 1 ? -(v - fv5) / fvk
+                  : lane == 2 ? (v - 60.f) / 12.f
+                  : lane == 3 ? -tq * tq
+                  : lane == 4 ? 2.f * za
+                  : lane == 5 ? (float)ETA * za
+                  : lane == 6 ? (float)(ETA - 1.0) * za
+                              : 0.f;
+  const float ex = expf(arg);
+  const float em = (lane == 0 || lane == 4) ? expm1f(arg) : 0.f;
+  const float ed = __shfl_sync(0xffffffffu, ex, 0), emd = __shfl_sync(0xffffffffu, em, 0);
+  const float ef1 = __shfl_sync(0xffffffffu, ex, 1), ef2 = __shfl_sync(0xffffffffu, ex, 2);
+  const float eq = __shfl_sync(0xffffffffu, ex, 3);
+  const float e2z = __shfl_sync(0xffffffffu, ex, 4), em2z = __shfl_sync(0xffffffffu, em, 4);
+  const float e1 = __shfl_sync(0xffffffffu, ex, 5), e2 = __shfl_sync(0xffffffffu, ex, 6);
+  // LCC gates (reesica.h:21-63)
+  const float dinf = 1.f / (1.f + ed);
+  float taudin = 1.f / ((-emd) / (0.035f * (v - dv5)) * dinf);
+  if ((vd < 0.0001) && (vd > -0.0001)) taudin = 0.035f * dvk / dinf;
+  const float fq = 1.f / (1.f + ef1) / (1.f + ef2);  // 1 - finf
+  const float finf = 1.f - fq;
+  const float taufin = 0.02f - 0.007f * eq;
+  k.alphad = dinf * taudin;
+  k.betad = (ed * dinf) * taudin;
+  k.alphaf = finf * taufin;
+  k.betaf = fq * taufin;
+  // ICaL (subroutine_cuda.c:231-247)
+  k.lcc_k = fabsf(za) < 0.001f ? (float)(2.0 * PCA * FARAD * GAMMAI)
+                               : (float)(4.0 * PCA * FARAD * GAMMAI) * za / em2z;
+  k.lcc_e2z_k = e2z / 1000.f;
+  // NCX (subroutine_cuda.c:56-67)
+  const float xn3 = xnai * xnai * xnai;
+  const float r = xnai / (float)KMNAI;
+  k.ncx_num_a = e1 * xn3 * (float)c.cao;
+  k.ncx_num_b = e2 * (float)(XNAO * XNAO * XNAO);
+  k.ncx_t1 = (float)(KMCAI * (XNAO * XNAO * XNAO)) * (1.f + r * r * r);
+  k.ncx_t3a = (float)(KMCAO + c.cao) * xn3;
+  k.ncx_den2 = 1.f + (float)KSAT * e2;
+  k.svica = (float)c.svica;
+  k.svncx = (float)c.svncx;
+  // build options (option_coef)
+  const double t = m.t;
+  k.sviup = (float)((c.iso && t >= 5.5 * c.pcl) ? c.sviup_iso : c.sviup_tot);
+  k.iso_add_lcc = c.iso && fm[4] < dt;
+  k.ncx_form = c.ncx_form;
+  k.ncx_ka_hill = c.ncx_form == RH_NCX_OLD || (c.ncx_form == RH_NCX_NOALLO && vd < -75);
+  k.ncx_t2b = (float)((KMNAI * KMNAI * KMNAI) * c.cao);
+  k.slowncx = c.slowncx;
+  k.bcg_a = (float)(BCG_G * vd);
+  k.bcg_b = (float)(BCG_G / 2. / FRT);
+  k.cao = (float)c.cao;
+  k.ku = (float)c.ku;
+  k.ku2 = (float)c.ku2;
+  k.kb = (float)c.kb;
+  k.dt = (float)dt;
+  k.rdt = (float)P.rdt;
+  k.dth = (float)P.dth;
+  k.rdt95 = (float)P.rdt95;
+  k.rdth95 = (float)P.rdth95;
+  k.reset_window = fm[0] < dt;
+  k.output_step = fm[1] < dt;
   k.perm = c.perm;
   k.cadist_step = k.output_step && fm[2] < dt && fm[3] < 500;
   return t < c.tend;

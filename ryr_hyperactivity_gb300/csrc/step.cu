@@ -123,12 +123,21 @@ __global__ void __launch_bounds__(32, 16) cell_kernel(StepArgs<R> a, int cell0, 
     const double t_step = m.t;  // the time the output record and statistics carry
     m.t = m.t + dt;             // :1083
     m.step += 1;
-    // coefficients of the next lattice update, with the qks update in spare
-    // slots of its rounds
+    // coefficients of the next lattice update: FP64 for the FP64 lattice
+    // (the qks update in spare slots of its rounds), FP32 for the FP32
+    // lattice (the qks update in one FP64 division beside it)
     StepCoef<double> kd;
-    QksStep qs{m.csubt, m.qks, pre.qks_num, pre.tauqks, 0.0};
-    const bool active = step_coef_warp(kd, m, cc, dt, fm + 1, scratch, &qs);
-    m.qks = m.qks + qs.dqks;
+    StepCoef<float> kf;
+    bool active;
+    if constexpr (sizeof(R) == 8) {
+      QksStep qs{m.csubt, m.qks, pre.qks_num, pre.tauqks, 0.0};
+      active = step_coef_warp(kd, m, cc, dt, fm + 1, scratch, &qs);
+      m.qks = m.qks + qs.dqks;
+    } else {
+      const double dqks = qks_increment_warp(m.csubt, m.qks, pre.qks_num, pre.tauqks, dt, scratch);
+      active = step_coef_warp_f32(kf, m, cc, dt, fm + 1, pre);
+      m.qks = m.qks + dqks;
+    }
     if (lane == 0) {
       if (a.stats) {  // per-beat detectors on the (t, V) sample of this step
         rh_beat_stats rec;
@@ -159,15 +168,16 @@ __global__ void __launch_bounds__(32, 16) cell_kernel(StepArgs<R> a, int cell0, 
         m.out_ncx = 0;
         m.out_ina = 0;
       }
-      StepCoef<float> kf;
-      convert_coef(kf, kd);
       if (!active) {
         dyn->done = 1;
         status |= RH_STATUS_DONE;
       }
       dyn->m = m;
-      dyn->cd = kd;
-      dyn->cf = kf;
+      if constexpr (sizeof(R) == 8) {
+        dyn->cd = kd;
+      } else {
+        dyn->cf = kf;
+      }
       dyn->status = status;
     }
   }
@@ -404,10 +414,12 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
 
   R p_cs = R(0), p_xicat = R(0), p_xinaca = R(0);
   uint32_t tstat = 0;  // this thread's status bits
-  double o[OUT ? NOUT : 1];
+  // output-step statistics of this thread's CRU, in the lattice precision
+  // (the integer ones are exact in FP32 too)
+  R o[OUT ? NOUT : 1];
   if (OUT) {
 #pragma unroll
-    for (int k = 0; k < NOUT; ++k) o[k] = 0.0;
+    for (int k = 0; k < NOUT; ++k) o[k] = R(0);
   }
 
   if (valid) {
@@ -859,27 +871,27 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     p_xinaca = xinaca;
 
     if (OUT && out_step) {
-      o[O_CP - P_STEP_END] = (double)cp;
-      o[O_CJSR - P_STEP_END] = (double)cjsr;
-      o[O_CJSRB - P_STEP_END] = (double)cjsrb;
-      o[O_CNSR - P_STEP_END] = (double)sum_cn;
-      o[O_CI - P_STEP_END] = (double)sum_ci;
-      o[O_PO - P_STEP_END] = (double)po;
-      o[O_NCB - P_STEP_END] = (double)ncb;
-      o[O_NCXFWD - P_STEP_END] = xinaca < R(0) ? (double)xinaca : 0.0;
-      o[O_CATF - P_STEP_END] = (double)sum_catf;
-      o[O_CATS - P_STEP_END] = (double)sum_cats;
-      o[O_CASR - P_STEP_END] = (double)sum_casr;
-      o[O_CAMYO - P_STEP_END] = (double)sum_camyo;
-      o[O_CACAL - P_STEP_END] = (double)sum_cacal;
-      o[O_LEAK - P_STEP_END] = (double)sum_lk;
-      o[O_UP - P_STEP_END] = (double)sum_up;
-      o[O_XIRE - P_STEP_END] = (double)xire;
-      o[O_ANCX - P_STEP_END] = (double)ancx;
-      o[O_CASAR - P_STEP_END] = (double)casar;
-      o[O_CASARH - P_STEP_END] = (double)casarh;
-      o[O_CASARJ - P_STEP_END] = (double)casarj;
-      o[O_CASARHJ - P_STEP_END] = (double)casarhj;
+      o[O_CP - P_STEP_END] = cp;
+      o[O_CJSR - P_STEP_END] = cjsr;
+      o[O_CJSRB - P_STEP_END] = cjsrb;
+      o[O_CNSR - P_STEP_END] = sum_cn;
+      o[O_CI - P_STEP_END] = sum_ci;
+      o[O_PO - P_STEP_END] = po;
+      o[O_NCB - P_STEP_END] = ncb;
+      o[O_NCXFWD - P_STEP_END] = xinaca < R(0) ? xinaca : R(0);
+      o[O_CATF - P_STEP_END] = sum_catf;
+      o[O_CATS - P_STEP_END] = sum_cats;
+      o[O_CASR - P_STEP_END] = sum_casr;
+      o[O_CAMYO - P_STEP_END] = sum_camyo;
+      o[O_CACAL - P_STEP_END] = sum_cacal;
+      o[O_LEAK - P_STEP_END] = sum_lk;
+      o[O_UP - P_STEP_END] = sum_up;
+      o[O_XIRE - P_STEP_END] = xire;
+      o[O_ANCX - P_STEP_END] = ancx;
+      o[O_CASAR - P_STEP_END] = casar;
+      o[O_CASARH - P_STEP_END] = casarh;
+      o[O_CASARJ - P_STEP_END] = casarj;
+      o[O_CASARHJ - P_STEP_END] = casarhj;
       o[O_NOU - P_STEP_END] = nou;
       o[O_NOB - P_STEP_END] = nob;
       o[O_NCU - P_STEP_END] = ncu;
@@ -902,7 +914,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
         for (int kk = 0; kk < 7; ++kk) o[O_TN1 - P_STEP_END + kk] = tn[kk];
       }
       o[O_SPARK - P_STEP_END] = nspark;
-      o[O_CIHIGH - P_STEP_END] = ci_high ? 1.0 : 0.0;
+      o[O_CIHIGH - P_STEP_END] = ci_high ? R(1) : R(0);
       if (cadist_step) {  // cadist row (:1009), post-step values in this CRU's slot
         double* r = a.out_cd + sh.cd_off + sh.cd_slot * (2 + 6 * (long long)sh.n) + 2 + 6 * (long long)q;
         r[0] = (double)cinext2[g].x;
@@ -970,16 +982,41 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   const uint32_t wst = __reduce_or_sync(0xffffffffu, tstat | (bad ? (uint32_t)RH_STATUS_NAN : 0u));
   if (OUT && out_step) {
     double* dst = a.partials + ((size_t)(a.tile_base + blockIdx.x) * NW + warp) * P_COUNT;
-#pragma unroll 1
-    for (int kk = 0; kk < NOUT; ++kk) {
-      double v = o[kk];
-      if (kk == O_CIHIGH - P_STEP_END) {
+    static_assert(O_CIHIGH - P_STEP_END == NOUT - 1 && NOUT - 1 == 32,
+                  "one summed statistic per lane, the ci flag last");
+    if constexpr (sizeof(R) == 4) {
+      // exact warp sums in 128-bit fixed point (integer adds, no FP64
+      // instruction); lane kk keeps statistic kk and converts it once; a
+      // non-finite (or out-of-range) value makes the statistic NaN
+      uint64_t mlo = 0, mhi = 0;
+      bool mbad = false;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
-      } else {
-        v = warp_sum(v);
+      for (int kk = 0; kk < NOUT - 1; ++kk) {
+        uint64_t lo, hi;
+        uint32_t bad = 0;
+        fx_warp_sum_f32(o[kk], lo, hi, bad);
+        const bool wbad = __any_sync(0xffffffffu, bad != 0u);
+        if (lane == kk) {
+          mlo = lo;
+          mhi = hi;
+          mbad = wbad;
+        }
       }
-      if (lane == 0) dst[P_STEP_END + kk] = v;
+      dst[P_STEP_END + lane] = mbad ? __longlong_as_double(0x7ff8000000000000ll) : fx_to_double(mlo, mhi);
+      const bool high = __any_sync(0xffffffffu, o[NOUT - 1] > R(0));
+      if (lane == 0) dst[P_STEP_END + NOUT - 1] = high ? 1.0 : 0.0;
+    } else {
+#pragma unroll 1
+      for (int kk = 0; kk < NOUT; ++kk) {
+        double v = o[kk];
+        if (kk == O_CIHIGH - P_STEP_END) {
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+        } else {
+          v = warp_sum(v);
+        }
+        if (lane == 0) dst[P_STEP_END + kk] = v;
+      }
     }
   }
   if (lane < 3) {
