@@ -244,6 +244,13 @@ int rh_drain_wholecell(rh_sim* sim, int32_t cell, double* rows, int32_t max_rec,
                        int32_t* nrec);
 int rh_drain_linescan(rh_sim* sim, int32_t cell, double* rows, int32_t max_rec,
                       int32_t* nrec);
+
+/* rh_drain_wholecell for every cell in one call (two device-to-host copies
+ * in all, instead of one round trip per cell and record): the records of
+ * cell c go to rows + c * max_rec * 45 and their number to nrec[c].  Replaces
+ * the reference's per-output-step host loop over the wholecell statistics
+ * (cuda_Cell_Detailed.cu:777-1072) for a batch of cells. */
+int rh_drain_wholecell_all(rh_sim* sim, double* rows, int32_t max_rec, int32_t* nrec);
 int rh_drain_stats(rh_sim* sim, int32_t cell, rh_beat_stats* out, int32_t max_rec,
                    int32_t* nrec);
 

@@ -1,12 +1,14 @@
 // rh_api.cu — host implementation of the C ABI in include/rh.h.
 //
-// Owns all device memory of a batch of cells, launches one fused step kernel
-// per time step (step.cu), replays windows of steps as captured CUDA graphs,
+// Owns all device memory of a batch of cells, launches the lattice update and
+// the cell update of each cell group per time step (step.cu), replays windows
+// of steps as captured CUDA graphs,
 // mirrors each cell's time on the host to know which steps are output steps,
 // and moves state and output records between host and device.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -70,6 +72,9 @@ struct rh_sim {
   std::vector<double> t_host;
   std::vector<char> active_host;
   std::vector<long long> drained_wc, drained_ls, drained_st, drained_cd;
+  // host staging of rh_drain_wholecell_all: record counters and the record ring
+  std::vector<long long> h_counts;
+  std::vector<double> h_ring;
   // graphs keyed by (window length, output-step bitmask)
   std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
   // timing
@@ -989,21 +994,60 @@ int rh_drain_wholecell(rh_sim* s, int32_t cell, double* rows, int32_t max_rec, i
   if (r) return r;
   if (!nrec || max_rec < 0 || (max_rec > 0 && !rows)) return RH_ERR_ARG;
   CK(cudaSetDevice(s->device));
-  CellDyn d;
-  if ((r = read_dyn(s, cell, &d))) return r;
+  CK(cudaStreamSynchronize(s->stream));
+  long long out_count = 0;  // only the record counter of the cell state
+  CK(cudaMemcpy(&out_count, reinterpret_cast<const char*>(s->d_dyn + cell) + offsetof(CellDyn, out_count),
+                sizeof out_count, cudaMemcpyDeviceToHost));
   const int cap = s->opts.output_capacity;
   long long first = s->drained_wc[cell];
-  if (d.out_count - first > cap) first = d.out_count - cap;  // overwritten records are lost
-  long long avail = d.out_count - first;
-  int cnt = (int)std::min<long long>(avail, max_rec);
-  for (int k = 0; k < cnt; ++k) {
-    long long slot = (first + k) % cap;
-    CK(cudaMemcpy(rows + (size_t)k * RH_WHOLECELL_COLS,
-                  s->d_out_wc + ((size_t)cell * cap + slot) * RH_WHOLECELL_COLS,
-                  sizeof(double) * RH_WHOLECELL_COLS, cudaMemcpyDeviceToHost));
+  if (out_count - first > cap) first = out_count - cap;  // overwritten records are lost
+  const long long avail = out_count - first;
+  const int cnt = (int)std::min<long long>(avail, max_rec);
+  // the ring slots [first, first + cnt) in at most two contiguous copies
+  const double* ring = s->d_out_wc + (size_t)cell * cap * RH_WHOLECELL_COLS;
+  int done = 0;
+  while (done < cnt) {
+    const int slot = (int)((first + done) % cap);
+    const int run = std::min(cnt - done, cap - slot);
+    CK(cudaMemcpy(rows + (size_t)done * RH_WHOLECELL_COLS, ring + (size_t)slot * RH_WHOLECELL_COLS,
+                  sizeof(double) * RH_WHOLECELL_COLS * run, cudaMemcpyDeviceToHost));
+    done += run;
   }
   s->drained_wc[cell] = first + cnt;
   *nrec = cnt;
+  return RH_OK;
+}
+
+int rh_drain_wholecell_all(rh_sim* s, double* rows, int32_t max_rec, int32_t* nrec) {
+  if (!s || !nrec || max_rec < 0 || (max_rec > 0 && !rows)) return RH_ERR_ARG;
+  CK(cudaSetDevice(s->device));
+  const int n = s->ncells, cap = s->opts.output_capacity;
+  const size_t ring_doubles = (size_t)n * cap * RH_WHOLECELL_COLS;
+  if (s->h_counts.size() != (size_t)n) s->h_counts.assign(n, 0);
+  if (s->h_ring.size() != ring_doubles) s->h_ring.assign(ring_doubles, 0.0);
+  // every cell's record counter (a strided copy out of the cell states) and
+  // the whole record ring, after the work queued so far
+  CK(cudaMemcpy2DAsync(s->h_counts.data(), sizeof(long long),
+                       reinterpret_cast<const char*>(s->d_dyn) + offsetof(CellDyn, out_count),
+                       sizeof(CellDyn), sizeof(long long), n, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaMemcpyAsync(s->h_ring.data(), s->d_out_wc, sizeof(double) * ring_doubles,
+                     cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  for (int c = 0; c < n; ++c) {
+    const long long out_count = s->h_counts[c];
+    long long first = s->drained_wc[c];
+    if (out_count - first > cap) first = out_count - cap;
+    const int cnt = (int)std::min<long long>(out_count - first, max_rec);
+    double* dst = rows + (size_t)c * max_rec * RH_WHOLECELL_COLS;
+    for (int k = 0; k < cnt; ++k) {
+      const size_t slot = (size_t)((first + k) % cap);
+      memcpy(dst + (size_t)k * RH_WHOLECELL_COLS,
+             s->h_ring.data() + ((size_t)c * cap + slot) * RH_WHOLECELL_COLS,
+             sizeof(double) * RH_WHOLECELL_COLS);
+    }
+    s->drained_wc[c] = first + cnt;
+    nrec[c] = cnt;
+  }
   return RH_OK;
 }
 

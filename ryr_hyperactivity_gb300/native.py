@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "librh.so")
 EXPORTS = [
     "rh_default_cell_params", "rh_default_run_opts", "rh_create", "rh_destroy", "rh_run_steps",
     "rh_run_to_end", "rh_lattice_step", "rh_set_ap_clamp", "rh_num_cells", "rh_cell_size", "rh_get_state",
-    "rh_set_state", "rh_get_membrane", "rh_set_membrane", "rh_drain_wholecell",
+    "rh_set_state", "rh_get_membrane", "rh_set_membrane", "rh_drain_wholecell", "rh_drain_wholecell_all",
     "rh_drain_linescan", "rh_drain_cadist", "rh_drain_stats", "rh_cell_status", "rh_checkpoint", "rh_restore",
     "rh_bytes_per_cru_step", "rh_kernel_timing", "rh_num_groups", "rh_last_error", "rh_format_wholecell",
     "rh_format_linescan", "rh_state_bytes", "rh_export_state", "rh_import_state",
@@ -55,6 +55,7 @@ def load() -> C.CDLL:
     L.rh_get_membrane.argtypes = [vp, C.c_int32, C.POINTER(Membrane)]
     L.rh_set_membrane.argtypes = [vp, C.c_int32, C.POINTER(Membrane)]
     L.rh_drain_wholecell.argtypes = [vp, C.c_int32, dp, C.c_int32, C.POINTER(C.c_int32)]
+    L.rh_drain_wholecell_all.argtypes = [vp, dp, C.c_int32, C.POINTER(C.c_int32)]
     L.rh_drain_linescan.argtypes = [vp, C.c_int32, dp, C.c_int32, C.POINTER(C.c_int32)]
     L.rh_set_ap_clamp.argtypes = [vp, C.c_int32, dp, C.c_int64]
     L.rh_drain_cadist.argtypes = [vp, C.c_int32, dp, C.c_int32, C.POINTER(C.c_int32)]

@@ -119,6 +119,14 @@ class Simulator:
                                            max_rec, C.byref(n)))
         return a[: n.value].copy()
 
+    def drain_wholecell_all(self, max_rec: int = 64) -> list[np.ndarray]:
+        """drain_wholecell of every cell in one library call."""
+        a = np.empty((self.ncells, max_rec, WHOLECELL_COLS))
+        n = np.zeros(self.ncells, dtype=np.int32)
+        self._ck(self.L.rh_drain_wholecell_all(self.h, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                               max_rec, n.ctypes.data_as(C.POINTER(C.c_int32))))
+        return [a[c, : n[c]].copy() for c in range(self.ncells)]
+
     def drain_linescan(self, cell: int = 0, max_rec: int = 4096) -> np.ndarray:
         lx = self.params[cell].nx - 2
         a = np.zeros((max_rec, lx, LINESCAN_COLS))

@@ -268,6 +268,31 @@ def test_cell_groups_give_identical_results():
                 np.testing.assert_array_equal(wc[c], wc0[c])
 
 
+def test_batched_drain_matches_per_cell_drain():
+    """rh_drain_wholecell_all returns, for every cell, the records
+    rh_drain_wholecell returns, and honours max_rec and the ring wrap-around
+    the same way (records beyond max_rec stay queued)."""
+    cells = [c1_params(nx=12 + 2 * i, ny=7 + i, nz=5, seed=5, cell_id=i) for i in range(4)]
+    out = []
+    for batched in (False, True):
+        with Simulator(cells, precision="mixed", output_capacity=8) as sim:
+            got = [[] for _ in cells]
+            for steps, max_rec in ((250, 64), (1100, 3), (100, 64)):
+                sim.run_steps(steps)  # 2, then 11 (3 drained, 8 left of which the ring keeps 8), then 1
+                if batched:
+                    for c, rows in enumerate(sim.drain_wholecell_all(max_rec)):
+                        got[c].append(rows)
+                else:
+                    for c in range(len(cells)):
+                        got[c].append(sim.drain_wholecell(c, max_rec))
+            out.append(got)
+    per_cell, batched = out
+    for c in range(len(cells)):
+        for a, b in zip(per_cell[c], batched[c]):
+            assert a.shape == b.shape and a.shape[0] > 0
+            np.testing.assert_array_equal(a, b)
+
+
 def _small_il():
     """The reference's small_il fixture cell (12x9x7, PCL 1000 ms, lqt/iso2
     build, curand seed 18) and its recorded cadist run."""
