@@ -193,8 +193,8 @@ class Simulator:
         return b.value
 
     def num_groups(self) -> int:
-        """Cell groups advanced on concurrent streams (one step-kernel launch
-        per group and lattice update)."""
+        """Cell groups advanced on concurrent streams (per group and time
+        step, a lattice launch and a cell-update launch)."""
         n = C.c_int32()
         self._ck(self.L.rh_num_groups(self.h, C.byref(n)))
         return n.value
