@@ -203,33 +203,25 @@ struct TileSmem {
   // The six cytosolic buffer fields (half of the state) are read straight
   // from global memory inside the sub-voxel loop: staging them as well costs
   // more in resident CTAs than it saves in latency.
-  static constexpr bool kStageBuf = false;
   static constexpr size_t kPlane = sizeof(V) * B;     // one pair plane
   static constexpr size_t kCi = 0;                     // V[4][B]
   static constexpr size_t kCn = 4 * kPlane;            // V[4][B]
-  static constexpr size_t kBuf = 8 * kPlane;           // V[6][4][B]: catf cats cacal casr camyo mgmyo
-  // The per-CRU scalars and integers (8 + 3 fields) are staged too when
-  // kStageSc; cs (index 8 of the scalar block) always is.
-#ifdef RH_STAGE_SC
-  static constexpr bool kStageSc = RH_STAGE_SC;
-#else
-  static constexpr bool kStageSc = kStage;
-#endif
-  static constexpr size_t kCs = kBuf + (kStageBuf ? 24 : 0) * kPlane;  // R[B]: cs
+  static constexpr size_t kCs = 8 * kPlane;            // R[B]: cs
+  // FP32 kernels stage the per-CRU scalars and integers (8 + 3 fields) too
   static constexpr size_t kSc = kCs + sizeof(R) * B;        // R[8][B]: cp cjsr cjsrb ancx casar casarh casarj casarhj
-  static constexpr size_t kLcc = kSc + (kStageSc ? 8 : 0) * sizeof(R) * B;  // uint2[B]
-  static constexpr size_t kRyr = kLcc + (kStageSc ? 8 : 0) * B;             // u32[B]
-  static constexpr size_t kWin = kRyr + (kStageSc ? 4 : 0) * B;             // u32[B]
+  static constexpr size_t kLcc = kSc + (kStage ? 8 : 0) * sizeof(R) * B;  // uint2[B]
+  static constexpr size_t kRyr = kLcc + (kStage ? 8 : 0) * B;             // u32[B]
+  static constexpr size_t kWin = kRyr + (kStage ? 4 : 0) * B;             // u32[B]
   // stencil halo of the tile (ci, cnsr; cs along z):
   //   y: V[dir][j][field][B], dir 1 = +lx (pairs 0, 2), dir 0 = -lx (pairs 1, 3)
   //   z: R[dir][pair][field][B], the pair half that faces the tile: the lower
   //      sub-voxel of the CRU above (dir 1), the upper one of the CRU below
   //   x: V[side][pair][field], side 0 = the CRU before the tile, 1 = after it
-  static constexpr size_t kHy = kWin + (kStageSc ? 4 : 0) * B;
+  static constexpr size_t kHy = kWin + (kStage ? 4 : 0) * B;
   static constexpr size_t kHz = kHy + 8 * kPlane;
   static constexpr size_t kHcs = kHz + 16 * sizeof(R) * B;  // R[dir][B]
   static constexpr size_t kHx = kHcs + 2 * sizeof(R) * B;  // V[2][4][2]
-  static constexpr size_t kBytes = kStage ? kHx + 16 * sizeof(V) : kBuf;
+  static constexpr size_t kBytes = kStage ? kHx + 16 * sizeof(V) : 8 * kPlane;
 };
 
 struct TileHeader {
@@ -252,10 +244,9 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
   extern __shared__ __align__(16) unsigned char dsm[];
   V(*s_ci2)[kBlock] = reinterpret_cast<V(*)[kBlock]>(dsm + TS::kCi);
   V(*s_cn2)[kBlock] = reinterpret_cast<V(*)[kBlock]>(dsm + TS::kCn);
-  V(*s_buf)[4][kBlock] = reinterpret_cast<V(*)[4][kBlock]>(dsm + TS::kBuf);
   R(*s_sc)[kBlock] = reinterpret_cast<R(*)[kBlock]>(dsm + TS::kSc);
   R* s_cs = reinterpret_cast<R*>(dsm + TS::kCs);
-  constexpr bool kSS = TS::kStageSc;
+  constexpr bool kSS = kStage;  // per-CRU scalars and integers staged
   uint2* s_lcc = reinterpret_cast<uint2*>(dsm + TS::kLcc);
   uint32_t* s_ryr = reinterpret_cast<uint32_t*>(dsm + TS::kRyr);
   uint32_t* s_win = reinterpret_cast<uint32_t*>(dsm + TS::kWin);
@@ -278,19 +269,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     // their copies start before the cell header arrives.  16-byte chunks:
     // a pair plane holds 2 CRUs per chunk, a 4-byte plane 4.
     const Lattice<R>& L = a.L;
-    const uint32_t S = (uint32_t)L.stride;
     constexpr int kTpp = kBlock / 2;  // threads per pair plane
     const int c2 = tid % kTpp, h2 = tid / kTpp;
-    if (TS::kStageBuf && 2 * c2 < cpad) {
-#pragma unroll
-      for (int k = 0; k < 12; ++k) {  // 6 buffers x 4 pair planes, two planes per round
-        const int f = k >> 1, pl = 2 * (k & 1) + h2;
-        const R* base = f == 0 ? L.catf : f == 1 ? L.cats : f == 2 ? L.cacal
-                      : f == 3 ? L.casr : f == 4 ? L.camyo : L.mgmyo;
-        cp_async16(&s_buf[f][pl][2 * c2],
-                   reinterpret_cast<const V*>(base) + pl * S + gt0 + 2 * c2);
-      }
-    }
     if (kSS && h2 == 0 && 2 * c2 < cpad) cp_async16(&s_lcc[2 * c2], L.lcc + gt0 + 2 * c2);
     constexpr int kTpq = kBlock / 4;  // threads per 4-byte plane
     const int c4 = tid % kTpq, h4 = tid / kTpq;
@@ -453,7 +433,7 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
     // the buffer fields of pair p + 1 load while pair p is computed (those
     // of pair 0 while the channel part runs)
     V nb0, nb1, nb2, nb3, nb4, nb5;
-    if (!TS::kStageBuf) {
+    {
       const V* b2 = reinterpret_cast<const V*>(L.catf);
       nb0 = b2[g];
       nb1 = reinterpret_cast<const V*>(L.cats)[g];
@@ -677,11 +657,8 @@ __global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArg
       const int by = p & 1, bx = p >> 1;
       const uint32_t gp = p * S + g;
       const V c = s_ci2[p][tid], n = s_cn2[p][tid];
-      constexpr bool kSB = TS::kStageBuf;
-      V catf = kSB ? s_buf[0][p][tid] : nb0, cats = kSB ? s_buf[1][p][tid] : nb1;
-      V cacal = kSB ? s_buf[2][p][tid] : nb2, casr = kSB ? s_buf[3][p][tid] : nb3;
-      V camyo = kSB ? s_buf[4][p][tid] : nb4, mgmyo = kSB ? s_buf[5][p][tid] : nb5;
-      if (!kSB && p < 3) {
+      V catf = nb0, cats = nb1, cacal = nb2, casr = nb3, camyo = nb4, mgmyo = nb5;
+      if (p < 3) {
         const uint32_t gq = gp + S;
         nb0 = catf2[gq], nb1 = cats2[gq], nb2 = cacal2[gq], nb3 = casr2[gq], nb4 = camyo2[gq];
         nb5 = mgmyo2[gq];
