@@ -103,6 +103,35 @@ def test_mixed_single_step_within_fp32_tolerance():
     assert max(errs.values()) <= FP32_RTOL, errs
 
 
+@pytest.mark.parametrize("v", [-85.0, -40.0, -5e-5, 0.3, 20.0])
+def test_mixed_two_full_steps_fp32_coefficients(v):
+    """The mixed cell update computes the next step's coefficients in FP32
+    (gating rates, GHK and NCX factors).  From an identical state at voltage v
+    (including |v| < 1e-4 mV, where taudin and the GHK factor take their
+    limiting forms), two full steps, the second on those coefficients, stay
+    within the FP32 tolerance of the FP64 oracle."""
+    p = c1_params()
+    st, m = rich_state(p, to_float32=True)
+    m.v = v
+    o = O.Oracle(p)
+    o.set_state(st)
+    o.set_membrane(m)
+    for _ in range(2):
+        o.step()
+    ref, mref = o.get_state(), o.get_membrane()
+    with Simulator(p, precision="mixed") as sim:
+        sim.set_state(0, st)
+        sim.set_membrane(0, m)
+        sim.run_steps(2)
+        got, mgot = sim.get_state(0), sim.get_membrane(0)
+    bad = count_mismatch(got, ref)
+    assert bad.mean() <= 0.02, f"{bad.sum()} of {bad.size} CRUs differ in counts"
+    errs = field_errors(got, ref, mask=~bad, fields=FLOAT_FIELDS)
+    assert max(errs.values()) <= 10 * FP32_RTOL, errs
+    assert abs(mgot.v - mref.v) <= 1e-3, (mgot.v, mref.v)
+    assert abs(mgot.xnai - mref.xnai) <= 1e-6 * abs(mref.xnai)
+
+
 def test_fp64_full_steps_match_oracle_outputs():
     p = c1_params()
     nsteps = 4400  # through the first upstroke (stimulus at t = 100 ms)
