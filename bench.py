@@ -148,8 +148,10 @@ def run_reference(args, rank, world):
             "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "cell_beats_per_s": cb,
-            "config": {"workload": "ensemble cell 0 (%dx%dx%d), host CPU" % (
-                cells[0].nx, cells[0].ny, cells[0].nz), "window_steps": WINDOW // 10},
+            "config": {"workload": "heterogeneous ensemble, 512 cells/GPU", "precision": "fp64",
+                       "sample": "cell 0 (%dx%dx%d), %d steps per bench step, host CPU" % (
+                           cells[0].nx, cells[0].ny, cells[0].nz, WINDOW // 10),
+                       "window_steps": WINDOW // 10},
             "cpu_baseline": {"value": val, "unit": "CRU-updates/s", "cores": threads,
                              "kind": "port", "sample": f"{args.steps} x {WINDOW // 10} steps of "
                              "one ensemble cell"},
@@ -239,8 +241,8 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
         "cell_beats_per_s": cell_beats,
-        "config": {"workload": f"heterogeneous ensemble, {args.cells} cells/GPU, {args.precision}",
-                   "cells": args.cells, "interior_crus": n_in, "window_steps": WINDOW,
+        "config": {"workload": f"heterogeneous ensemble, {args.cells} cells/GPU",
+                   "precision": args.precision, "cells": args.cells, "interior_crus": n_in, "window_steps": WINDOW,
                    "step": "one output window = 100 lattice updates of every cell",
                    "l2": f"state {sim.state_bytes() / 1e9:.2f} GB > 129 MB L2, no flush",
                    "parallelism": f"cells sharded, {world} GPU(s)",
