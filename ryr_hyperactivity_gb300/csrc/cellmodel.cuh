@@ -1,6 +1,6 @@
 // cellmodel.cuh — whole-cell part of a time step, FP64: the membrane
 // currents, gates, [Na]i and V (cuda_Cell_Detailed.cu:458-739, run on the
-// host every step in the reference, here by the last CTA of each cell), the
+// host every step in the reference, here by the cell update on the GPU), the
 // per-cell voltage coefficients of the next lattice update, and the 45
 // wholecell output columns (:1031-1072).
 #pragma once

@@ -43,8 +43,8 @@ struct rh_sim {
   int ts = 0;
   // Cell groups: contiguous cell ranges of about equal CRU count, each with
   // its own stream.  A window of steps runs as one graph with a branch per
-  // group, so one group's end-of-step tail (its last CTAs and the cell
-  // updates they run) overlaps the other groups' lattice work.
+  // group, so one group's end-of-step tail (its last lattice CTAs and its
+  // cell update) overlaps the other groups' lattice work.
   int ngroups = 1;
   std::vector<int> group_cell;  // group g holds cells [group_cell[g], group_cell[g+1])
   std::vector<char> group_opt;  // group g has a cell with lattice build options
