@@ -65,8 +65,8 @@ def test_fp64_protocol_matches_oracle(variant):
 
 def test_protocols_in_one_batch():
     """Cells of every protocol advance together in one batch (the same
-    launches per step), each
-    with its own voltage source, and each matches its own oracle."""
+    launches per step), each with its own voltage source, and each matches
+    its own oracle."""
     cells = [c1_params(nx=9, ny=6, nz=5, seed=4, cell_id=i, pcl_ms=200.0, nbeats=2, protocol=pr,
                        clamp_mv=-20.0, perm=int(pr == "paced" and i == 6))
              for i, pr in enumerate(["paced", "nopacing", "vclamp", "brownvclamp", "apclamp",
