@@ -242,7 +242,8 @@ def main():
         "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
         "cell_beats_per_s": cell_beats,
         "config": {"workload": f"heterogeneous ensemble, {args.cells} cells/GPU",
-                   "precision": args.precision, "cells": args.cells, "interior_crus": n_in, "window_steps": WINDOW,
+                   "precision": args.precision, "cells": args.cells, "interior_crus": n_in,
+                   "window_steps": WINDOW,
                    "step": "one output window = 100 lattice updates of every cell",
                    "l2": f"state {sim.state_bytes() / 1e9:.2f} GB > 129 MB L2, no flush",
                    "parallelism": f"cells sharded, {world} GPU(s)",
