@@ -58,6 +58,20 @@ def test_create_rejects_bad_arguments_without_gpu_work():
     assert b"lattice" in buf.value
 
 
+def test_calls_on_a_null_handle_are_rejected():
+    """Every per-simulator entry point returns RH_ERR_ARG for a NULL handle
+    (no device work is attempted)."""
+    import ctypes as C
+    L = native.load()
+    n = C.c_int32()
+    rows = (C.c_double * 45)()
+    assert L.rh_run_steps(None, 10) == -1
+    assert L.rh_drain_wholecell(None, 0, rows, 1, C.byref(n)) == -1
+    assert L.rh_drain_wholecell_all(None, rows, 1, C.byref(n)) == -1
+    assert L.rh_num_cells(None, C.byref(n)) == -1
+    assert L.rh_num_groups(None, C.byref(n)) == -1
+
+
 def test_record_formats_match_reference():
     from oracle import oracle as O
     from ryr_hyperactivity_gb300.sim import format_linescan, format_wholecell
