@@ -136,3 +136,22 @@ def test_thread_count_does_not_change_results():
         outs.append(wc)
     O.lib().orc_set_threads(0)
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+def test_closed_cell_conserves_total_ca():
+    """With ICaL and NCX off (ica_scale = ncx_scale = 0) no Ca crosses the
+    sarcolemma, so the Total_Ca column (col 45, :1031-1039, every compartment
+    weighted by its volume) stays constant.  The model holds it to a few 1e-8
+    relative through an action potential and its Ca transient (release,
+    uptake, buffering and diffusion exchange Ca between compartments only);
+    after the transient it is constant to rounding.  The FP64 GPU path follows
+    these records to 1e-9 (tests/test_gpu_parity.py)."""
+    from tests.gpu_helpers import c1_params
+    p = c1_params(ica_scale=0.0, ncx_scale=0.0)
+    o = O.Oracle(p)
+    n, wc, _ = o.run(8000)
+    assert n == 8000 and len(wc) == 80
+    assert wc[:, 2].max() > 0  # an action potential ran
+    tc = wc[:, 44]
+    assert np.max(np.abs(tc - tc[0])) <= 1e-7 * tc[0]
+    assert np.max(np.abs(tc[60:] - tc[60])) <= 1e-12 * tc[0]
