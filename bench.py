@@ -90,6 +90,15 @@ def _peaks():
         return {}
 
 
+def _fp64_profile():
+    """FP64-pipe utilisation of the FP64 lattice kernel from its committed ncu
+    summary (profiles/step_kernel_fp64.json)."""
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "step_kernel_fp64.json")))
+    except Exception:
+        return None
+
+
 def _traffic_profile():
     try:
         return json.load(open(os.path.join(ROOT, "profiles", "step_kernel_traffic.json")))
@@ -97,64 +106,108 @@ def _traffic_profile():
         return None
 
 
-def cpu_baseline(seconds: float = 12.0, threads: int | None = None) -> dict:
-    """The CPU oracle (C restatement, OpenMP over CRUs) on one mean-size cell
-    of the ensemble (80x16x8, 6552 interior CRUs), run in 100-step windows
-    for about `seconds`."""
-    from oracle import oracle as O
-    from ryr_hyperactivity_gb300.workloads import STAB
-    from ryr_hyperactivity_gb300.abi import cell_params
+# The CPU baseline: the reference's own update routines compiled for the host
+# (oracle/build_ref.sh, variant bench_mean: Compute, the host ODE and the
+# writers of cuda_Cell_Detailed.cu, OpenMP over the lattice sites) on the mean
+# lattice of the ensemble, 80x16x8 (6552 interior CRUs), PCL 1750 ms, with the
+# RyR-hyperactive argv of run.sh:9 and Ku2 = 2 (the ensemble's mean).  Where
+# that build is absent the oracle port (the same update restated in C, pinned
+# byte for byte to the reference build) runs instead.
+MEAN_CELL = dict(nx=80, ny=16, nz=8, pcl_ms=1750.0)
+MEAN_ARGS = [1.0, 740, 1.0, 3.333, 0.0, 18.0, 0.7, 2.0]
+REF_SAMPLE_STEPS = 1000  # lattice updates per reference sample (one process run)
 
-    threads = threads or os.cpu_count() or 1
-    p = cell_params(nx=82, ny=18, nz=10, nbeats=20, pcl_ms=1750.0, lqt=0, iso2=1,
-                    ikr_scale=0.5, seed=1, cell_id=0, **STAB)
-    o = O.Oracle(p, threads=threads)
-    o.run(WINDOW)  # warm
-    n = o.n
-    t0 = time.perf_counter()
-    steps = 0
-    while time.perf_counter() - t0 < seconds:
-        o.run(WINDOW)
-        steps += WINDOW
-    el = time.perf_counter() - t0
-    return {"value": n * steps / el, "unit": "CRU-updates/s", "cores": threads, "kind": "port",
-            "sample": f"one 80x16x8 cell (6552 interior CRUs), {steps} steps, {el:.1f} s",
-            "cell_beats_per_s": steps * DT / 1750.0 / el}
+
+def _mean_interior() -> int:
+    return (MEAN_CELL["nx"] - 2) * (MEAN_CELL["ny"] - 2) * (MEAN_CELL["nz"] - 2)
+
+
+def _reference_exe():
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_bench_mean")
+    return exe if os.access(exe, os.X_OK) else None
+
+
+class CpuSampler:
+    """Runs bounded samples of the mean-size cell on the host cores: the
+    reference build when present ("reference"), else the oracle port."""
+
+    def __init__(self, threads: int | None = None):
+        self.threads = threads or os.cpu_count() or 1
+        self.exe = _reference_exe()
+        self.kind = "reference" if self.exe else "port"
+        self.n = _mean_interior()
+        self._o = None
+        self._dir = None
+
+    def sample(self, steps: int) -> float:
+        """Runs `steps` lattice updates; returns the elapsed seconds."""
+        if self.exe:
+            import tempfile
+            if self._dir is None:
+                self._dir = tempfile.mkdtemp(prefix="rh_ref_")
+            env = dict(os.environ, REF_MAX_STEPS=str(int(steps)),
+                       OMP_NUM_THREADS=str(self.threads))
+            t0 = time.perf_counter()
+            subprocess.run([self.exe, "0", "b"] + [str(a) for a in MEAN_ARGS], cwd=self._dir,
+                           env=env, check=True, stdout=subprocess.DEVNULL)
+            return time.perf_counter() - t0
+        if self._o is None:
+            from oracle import oracle as O
+            from ryr_hyperactivity_gb300.abi import cell_params
+            from ryr_hyperactivity_gb300.workloads import HYPER
+            d = dict(HYPER, ku2=2.0)
+            p = cell_params(nbeats=20, lqt=0, iso2=1, seed=1, cell_id=0, **MEAN_CELL, **d)
+            self._o = O.Oracle(p, threads=self.threads)
+        t0 = time.perf_counter()
+        self._o.run(steps)
+        return time.perf_counter() - t0
+
+    def describe(self, steps: int, seconds: float) -> str:
+        what = ("the reference's host build (oracle/_ref/ref_bench_mean), one process run per "
+                "sample" if self.kind == "reference" else "the oracle port")
+        return (f"{what}: one 80x16x8 cell ({self.n} interior CRUs), {steps} steps in "
+                f"{REF_SAMPLE_STEPS}-step samples, {seconds:.1f} s")
+
+
+def cpu_baseline(seconds: float = 12.0, threads: int | None = None) -> dict:
+    """The CPU baseline on the mean-size ensemble cell for about `seconds`."""
+    cs = CpuSampler(threads)
+    cs.sample(100)  # warm
+    el, steps = 0.0, 0
+    while el < seconds:
+        el += cs.sample(REF_SAMPLE_STEPS)
+        steps += REF_SAMPLE_STEPS
+    return {"value": cs.n * steps / el, "unit": "CRU-updates/s", "cores": cs.threads,
+            "kind": cs.kind, "sample": cs.describe(steps, el),
+            "cell_beats_per_s": steps * DT / MEAN_CELL["pcl_ms"] / el}
 
 
 def run_reference(args, rank, world):
-    """Reference arm: the reference's update routines on the host cores (the
-    oracle restatement, pinned byte-for-byte to the reference compiled for
-    the host), same metric and unit, bounded sample per step."""
+    """Reference arm: the reference's update routines on the host cores, same
+    metric and unit as the GPU arm; each bench step is one bounded sample of
+    the ensemble's mean-size cell (REF_SAMPLE_STEPS lattice updates)."""
     if rank != 0:
         return
-    from oracle import oracle as O
-    from ryr_hyperactivity_gb300.workloads import config3_cells, interior
-
-    threads = os.cpu_count() or 1
-    cells = config3_cells(512)[:1]  # one cell of the ensemble per bench step sample
-    o = O.Oracle(cells[0], threads=threads)
+    cs = CpuSampler()
     for _ in range(args.warmup):
-        o.run(10)
-    t0 = time.perf_counter()
+        cs.sample(REF_SAMPLE_STEPS // 10)
+    el = 0.0
     for _ in range(args.steps):
-        o.run(WINDOW // 10)
-    el = time.perf_counter() - t0
-    upd = interior(cells[0]) * (WINDOW // 10) * args.steps
-    val = upd / el
-    cb = (WINDOW // 10) * DT / cells[0].pcl_ms * args.steps / el
+        el += cs.sample(REF_SAMPLE_STEPS)
+    steps = REF_SAMPLE_STEPS * args.steps
+    val = cs.n * steps / el
+    cb = steps * DT / MEAN_CELL["pcl_ms"] / el
     line = {"impl": "reference", "metric": "CRU-updates/s", "value": val, "unit": "CRU-updates/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "cell_beats_per_s": cb,
             "config": {"workload": "heterogeneous ensemble, 512 cells/GPU", "precision": "fp64",
-                       "sample": "cell 0 (%dx%dx%d), %d steps per bench step, host CPU" % (
-                           cells[0].nx, cells[0].ny, cells[0].nz, WINDOW // 10),
-                       "window_steps": WINDOW // 10},
-            "cpu_baseline": {"value": val, "unit": "CRU-updates/s", "cores": threads,
-                             "kind": "port", "sample": f"{args.steps} x {WINDOW // 10} steps of "
-                             "one ensemble cell"},
+                       "sample": "the ensemble's mean-size cell (80x16x8), %d lattice updates "
+                                 "per bench step, host CPU" % REF_SAMPLE_STEPS,
+                       "window_steps": REF_SAMPLE_STEPS},
+            "cpu_baseline": {"value": val, "unit": "CRU-updates/s", "cores": cs.threads,
+                             "kind": cs.kind, "sample": cs.describe(steps, el)},
             "e2e": {"value": val, "unit": "CRU-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -198,8 +251,11 @@ def main():
 
     cells = config3_cells(args.cells, first_id=rank * args.cells)
     n_in = sum(interior(p) for p in cells)
+    # the per-beat detectors (APD90, EAD, peak [Ca]i, SR load, sparks) run in
+    # the timed region, as an ensemble study needs them
     sim = Simulator(cells, precision=args.precision, device=local, window_steps=WINDOW,
-                    track_stats=0, block_size=args.tile, cell_groups=args.groups)
+                    track_stats=1, stats_capacity=64, block_size=args.tile,
+                    cell_groups=args.groups)
     bpc = sim.bytes_per_cru_step()
     for _ in range(args.warmup):
         sim.run_steps(WINDOW)
@@ -302,6 +358,35 @@ def main():
             "workload": "100x20x10 single cell, FP64", "cru_updates_per_s": v64,
             "cell_beats_per_s": cb64, "kernel_ms": k64 / max(l64, 1),
             "mixed_batched_over_fp64_single_cell_cell_beats": cell_beats / world / cb64}
+    # the same 512-cell ensemble with every field and operation in FP64
+    # (batched FP64): its lattice kernel is bound by the FP64 pipe
+    if not args.no_fp64 and rank == 0 and args.precision == "mixed":
+        sb = Simulator(cells, precision="fp64", device=local, window_steps=WINDOW, track_stats=1,
+                       stats_capacity=64, block_size=args.tile, cell_groups=args.groups)
+        sb.run_steps(WINDOW)
+        sb.kernel_timing()
+        torch.cuda.synchronize()
+        nwb = 2
+        for _ in range(nwb):
+            sb.run_steps(WINDOW)
+        torch.cuda.synchronize()
+        lb, kb = sb.kernel_timing()
+        bpc64 = sb.bytes_per_cru_step()
+        sb.close()
+        vb = n_in * WINDOW * nwb / (kb / 1e3)
+        cbb = sum(WINDOW * DT / p.pcl_ms for p in cells) * nwb / (kb / 1e3)
+        ach64 = bpc64 * n_in / (kb / 1e3 / max(lb, 1)) / 1e9
+        fp64_prof = _fp64_profile()
+        result["fp64_batched"] = {
+            "workload": f"heterogeneous ensemble, {args.cells} cells, FP64",
+            "cru_updates_per_s": vb, "cell_beats_per_s": cbb, "kernel_ms": kb / max(lb, 1),
+            "roofline": {"bound": "fp64", "hbm_achieved": ach64, "hbm_peak": peak,
+                         "hbm_frac": (ach64 / peak) if peak else None,
+                         "bytes_per_cru_update": bpc64,
+                         "fp64_pipe_pct_of_peak_ncu": fp64_prof.get("fp64_pipe_pct") if fp64_prof
+                         else None,
+                         "fp64_evidence": fp64_prof.get("source") if fp64_prof else None},
+            "mixed_over_fp64_batched_cell_beats": cell_beats / world / cbb}
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline()
     if rank == 0:

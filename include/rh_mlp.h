@@ -64,10 +64,12 @@ int rh_mlp_last_error(const rh_mlp* m, char* buf, size_t n);
  * RH_MLP_NOALLOC_SCRATCH_BYTES (4 MiB) per device, held from the library's
  * loading until process exit.  n above RH_MLP_NOALLOC_MAX_BATCH is rejected
  * with RH_ERR_ARG and a message in err (err may be NULL).  The first call on
- * a device looks up that array's device address (one-time set-up); make that
- * first call before any stream capture.  All calls on a device share the
- * array: two calls whose work overlaps on the GPU (different streams, or
- * different threads without ordering) race and give wrong results.  Each
+ * a device looks up that array's device address (one-time set-up, repeated
+ * when the call comes from another context of that device, e.g. after
+ * cudaDeviceReset); make that first call before any stream capture.  All
+ * calls on a device share the array: two calls whose work overlaps on the
+ * GPU (different streams, or different threads without ordering) race and
+ * give wrong results.  Each
  * call writes every scratch value it reads, so nothing left by an earlier
  * call reaches the result. */
 #define RH_MLP_NOALLOC_MAX_BATCH 4096

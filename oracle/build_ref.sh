@@ -2,8 +2,9 @@
 # build_ref.sh — compiles the reference program for the host CPU (test oracle
 # pin; TEST INFRASTRUCTURE ONLY).
 #
-# Reads the reference sources where they lie (REF_SRC, default /root/reference)
-# and writes only into oracle/_ref/ (git-ignored):
+# Reads the reference sources where they lie (the directory named by the
+# REF_SRC environment variable; there is no default) and writes only into
+# oracle/_ref/ (git-ignored):
 #   oracle/_ref/gen/ref_fixA.cpp   cuda_Cell_Detailed.cu with
 #       - the "fixA" repair: lines 1475-1597 (the second, duplicated dyad /
 #         cytosol block) and the stray brace on line 1692 deleted, which is the
@@ -17,7 +18,8 @@
 #       - the NCX call of Compute (:1296) routed through REF_NCX, so that a
 #         variant can select the reference's oldncx or ncx_noallo instead.
 #   oracle/_ref/gen/*.c, reesica.h   the three device files it includes, copied
-#       so that the generated program builds where the reference is absent.
+#       so that the generated program builds where the reference is absent
+#       (REF_SRC unset: the generated copy is used when it exists).
 #   oracle/_ref/ref_<variant>         host executables (g++ -fopenmp).
 # The LCC loop of Compute tests lcc[ll] < 16 before ll < 8 (:1253), so a CRU
 # with all eight slots filled (iso after 5.5 PCL, randomlcc) reads lcc[8], one
@@ -28,13 +30,13 @@
 # Usage: build_ref.sh [variant ...]   (default: all variants below)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF_SRC="${REF_SRC:-/root/reference}"
+REF_SRC="${REF_SRC:-}"
 OUT="$HERE/_ref"
 GEN="$OUT/gen"
 CXX="${CXX:-g++}"
 mkdir -p "$GEN"
 
-if [ -f "$REF_SRC/cuda_Cell_Detailed.cu" ]; then
+if [ -n "$REF_SRC" ] && [ -f "$REF_SRC/cuda_Cell_Detailed.cu" ]; then
   sed -e '1475,1597d' -e '1692d' "$REF_SRC/cuda_Cell_Detailed.cu" |
     sed -E \
       -e 's/^#define (nbeat|tperid|nx|ny|nz)([[:space:]]+)([^/]*)(.*)$/#ifndef \1\n#define \1 \3 \4\n#endif/' \
@@ -48,7 +50,7 @@ if [ -f "$REF_SRC/cuda_Cell_Detailed.cu" ]; then
   for f in subroutine_cuda.c reesica.h buffers.c; do cp "$REF_SRC/$f" "$GEN/$f"; done
   mv "$GEN/ref_fixA.cpp.tmp" "$GEN/ref_fixA.cpp"
 elif [ ! -f "$GEN/ref_fixA.cpp" ]; then
-  echo "build_ref.sh: reference sources not found at $REF_SRC and no generated copy in $GEN" >&2
+  echo "build_ref.sh: no reference sources (REF_SRC='$REF_SRC') and no generated copy in $GEN" >&2
   exit 3
 fi
 
@@ -66,6 +68,9 @@ declare -A VARIANTS=(
   [small_il]="-Dnx=12 -Dny=9 -Dnz=7 -Dnbeat=1 -Dtperid=1000.0 -DREF_LINESCAN_JZ=5 -Diso2 -Dlqt"
   # the shipped 64x28x12 make-il build
   [default_il]="-Diso2 -Dlqt -DREF_LINESCAN_JZ=5"
+  # the mean lattice of the 512-cell heterogeneous ensemble (80x16x8, 6552
+  # interior CRUs), iso2 build, PCL 1750 ms: the CPU baseline of bench.py
+  [bench_mean]="-Dnx=80 -Dny=16 -Dnz=8 -Dnbeat=20 -Dtperid=1750.0 -DREF_LINESCAN_JZ=5 -Diso2"
   # small_il with the reference's cadist_ writer enabled (#define outputcadist)
   [small_il_cd]="-Dnx=12 -Dny=9 -Dnz=7 -Dnbeat=1 -Dtperid=1000.0 -DREF_LINESCAN_JZ=5 -Diso2 -Dlqt -Doutputcadist"
   # the voltage protocols and cell preparations of the reference's build

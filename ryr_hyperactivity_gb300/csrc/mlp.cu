@@ -9,6 +9,7 @@
 // (mma.sync m16n8k16, BF16 x BF16 -> FP32): forward Z = A W^T, backward
 // dA = dZ W and dW = dZ^T A.  Padded shapes: layer 1 K = 16 (4 inputs +
 // zeros), layer 4 N = 8 (3 outputs + zeros).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -510,8 +511,39 @@ __global__ void weights_to_bf16(const float* w, __nv_bfloat16* wb, int n, int k,
 }
 
 constexpr int kMaxDevices = 64;
+// The device address of the scratch array belongs to one CUDA context.  The
+// cache holds it per device together with the id of the context that was
+// current when it was looked up; a call from another context on that device
+// (a context the caller made current, or the primary context created anew
+// after cudaDeviceReset) looks it up again.
 std::mutex g_scratch_mu;
 void* g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
+
+// Id of the calling thread's current context (cuCtxGetCurrent + cuCtxGetId,
+// reached through the runtime's driver entry points so that the library does
+// not link the driver library itself); false where it cannot be had.
+bool current_context_id(unsigned long long* id) {
+  using GetCurrentFn = CUresult (*)(CUcontext*);
+  using GetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetIdFn>(f);
+  });
+  CUcontext ctx = nullptr;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+  return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 void na_msg(char* err, size_t len, const char* fmt, ...) __attribute__((format(printf, 3, 4)));
 void na_msg(char* err, size_t len, const char* fmt, ...) {
@@ -561,12 +593,18 @@ extern "C" int rh_mlp_forward_noalloc(const float* d_params, const float* d_x, i
            dev);
     return RH_ERR_ARG;
   }
-  // Set-up, once per device, with that device current: the scratch array's
-  // device address.  Later calls reuse the cached address.
+  // Set-up, once per device (and context), with that device current: the
+  // scratch array's device address.  Later calls from the same context reuse
+  // the cached address.
   void* base = nullptr;
   {
+    // the pointer checks above ran runtime calls on this thread, so its
+    // context is current; without a context id the address is looked up
+    // on every call
+    unsigned long long ctx = 0;
+    const bool known_ctx = current_context_id(&ctx);
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
+    if (!g_scratch_addr[dev] || !known_ctx || g_scratch_ctx[dev] != ctx) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_forward_scratch);
       if (e != cudaSuccess || !p) {
@@ -575,6 +613,7 @@ extern "C" int rh_mlp_forward_noalloc(const float* d_params, const float* d_x, i
         return RH_ERR_CUDA;
       }
       g_scratch_addr[dev] = p;
+      g_scratch_ctx[dev] = known_ctx ? ctx : 0;
     }
     base = g_scratch_addr[dev];
   }

@@ -1,8 +1,9 @@
 """Generates the golden fixtures in this directory from the reference program
 compiled for the host (oracle/_ref, built by oracle/build_ref.sh from the
-reference sources).  Run here, where the reference sources exist:
+reference sources).  Run where the reference sources exist, REF_SRC naming
+their directory:
 
-    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+    REF_SRC=<reference sources> bash oracle/build_ref.sh && python tests/golden/make_golden.py
 
 Fixtures (all produced by running the reference's own code):
   ref_<variant>_wholetest_head.txt   first wholetest_ lines of the run

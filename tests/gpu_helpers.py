@@ -109,3 +109,44 @@ def variant_params(spec: dict):
     a = spec["args"]
     return cell_params(clamp_mv=a[0], cjsr_basal=a[1], ncx_scale=a[2], ku=a[3], r1=a[4], kb=a[5],
                        ica_scale=a[6], ku2=a[7], seed=spec["seed"], **spec["cell"])
+
+
+def assert_text_files_match(got: str, want: str, rtol: float = 1e-5, atol: float = 2e-6):
+    """Output files printed as the reference prints them (wholetest_,
+    linescan_): the same lines, blank lines included, each with the same
+    fields in the same places (the same single and double spaces), and the
+    numbers equal within rtol/atol (atol covers the last printed digit of a
+    %f field)."""
+    a_lines, b_lines = got.splitlines(), want.splitlines()
+    assert len(a_lines) == len(b_lines), (len(a_lines), len(b_lines))
+    for k, (a, b) in enumerate(zip(a_lines, b_lines)):
+        fa, fb = a.split(" "), b.split(" ")
+        assert len(fa) == len(fb), (k, a, b)
+        for x, y in zip(fa, fb):
+            assert (x == "") == (y == ""), (k, a, b)
+        va = np.array([float(x) for x in fa if x])
+        vb = np.array([float(x) for x in fb if x])
+        np.testing.assert_allclose(va, vb, rtol=rtol, atol=atol, err_msg=f"line {k}")
+
+
+def flux_errors(got: HostState, ref: HostState, mask=None):
+    """Per-flux (diagnostic) error relative to that flux's largest magnitude
+    in the cell.  A flux is a difference of larger terms (the GHK LCC current
+    lcc_k (cpx e2z - cao) crosses zero near its reversal, SERCA is uptake
+    minus back-flux), so in FP32 its rounding error scales with those terms,
+    not with the difference; what reaches the concentrations is that error
+    against the flux's scale."""
+    n = ref.n
+    out = {}
+    for f in DIAG:
+        g, r = got[f], ref[f]
+        if g.size == 8 * n:
+            g, r = g.reshape(8, n), r.reshape(8, n)
+            if mask is not None:
+                g, r = g[:, mask], r[:, mask]
+        elif mask is not None:
+            g, r = g[mask], r[mask]
+        scale = max(float(np.max(np.abs(r))) if r.size else 0.0, 1e-300)
+        out[f] = float(np.max(np.abs(g - r))) / scale if r.size else 0.0
+    return out
+

@@ -1,5 +1,6 @@
-"""The reference arm of bench.py (the oracle on the host cores) prints one
-JSON line with the fields and units of the GPU arm; runs on CPU."""
+"""The reference arm of bench.py (the reference's host build, or the oracle
+port where that build is absent, on the host cores) prints one JSON line with
+the fields and units of the GPU arm; runs on CPU."""
 import json
 import os
 import subprocess
@@ -19,6 +20,6 @@ def test_reference_arm_prints_the_contract_line():
     assert d["metric"] == "CRU-updates/s" and d["unit"] == "CRU-updates/s"
     assert d["higher_is_better"] is True and d["value"] > 0
     assert d["config"]["workload"] == "heterogeneous ensemble, 512 cells/GPU"
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["kind"] in ("reference", "port") and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["e2e"]["value"] == d["value"]

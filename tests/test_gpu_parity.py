@@ -1,8 +1,10 @@
 """Parity of the CUDA path (through the C ABI) with the CPU oracle.
 
-Bars (stated in the benchmark spec): from identical state, one lattice step
-gives bit-identical RyR/LCC counts and concentrations within 1e-10 relative
-in FP64; within 1e-5 relative in the mixed (FP32 lattice) path.
+Bars: from identical state, one lattice step gives bit-identical RyR/LCC
+counts and concentrations within 1e-10 relative in FP64; in the mixed (FP32
+lattice) path concentrations within 1e-5 relative and the per-CRU fluxes
+within 1e-5 of each flux's largest magnitude (a flux is a difference of larger
+terms, so FP32 rounding scales with the terms).
 """
 import os
 import subprocess
@@ -15,8 +17,8 @@ from oracle import oracle as O
 from ryr_hyperactivity_gb300.abi import cell_params
 from ryr_hyperactivity_gb300.sim import Simulator
 
-from tests.gpu_helpers import (COUNT_FIELDS, DIAG, FLOAT_FIELDS, c1_params, count_mismatch,
-                          field_errors, rich_state)
+from tests.gpu_helpers import (COUNT_FIELDS, DIAG, FLOAT_FIELDS, assert_text_files_match,
+                               c1_params, count_mismatch, field_errors, flux_errors, rich_state)
 
 pytestmark = pytest.mark.gpu
 
@@ -99,8 +101,10 @@ def test_mixed_single_step_within_fp32_tolerance():
     # float uniforms (24 bit) decide a Poisson/LCC comparison differently only
     # when the two sides are within ~6e-8 of each other
     assert bad.mean() <= 0.01, f"{bad.sum()} of {bad.size} CRUs differ in counts"
-    errs = field_errors(got, ref, mask=~bad)
+    errs = field_errors(got, ref, mask=~bad, fields=FLOAT_FIELDS)
     assert max(errs.values()) <= FP32_RTOL, errs
+    ferrs = flux_errors(got, ref, mask=~bad)
+    assert max(ferrs.values()) <= FP32_RTOL, ferrs
 
 
 @pytest.mark.parametrize("v", [-85.0, -40.0, -5e-5, 0.3, 20.0])
@@ -125,9 +129,11 @@ def test_mixed_two_full_steps_fp32_coefficients(v):
         sim.run_steps(2)
         got, mgot = sim.get_state(0), sim.get_membrane(0)
     bad = count_mismatch(got, ref)
+    print(f"v {v}: count mismatch fraction {bad.mean():.2e}")
     assert bad.mean() <= 0.02, f"{bad.sum()} of {bad.size} CRUs differ in counts"
     errs = field_errors(got, ref, mask=~bad, fields=FLOAT_FIELDS)
-    assert max(errs.values()) <= 10 * FP32_RTOL, errs
+    print({k: f"{e:.2e}" for k, e in errs.items()})
+    assert max(errs.values()) <= FP32_RTOL, errs
     assert abs(mgot.v - mref.v) <= 1e-3, (mgot.v, mref.v)
     assert abs(mgot.xnai - mref.xnai) <= 1e-6 * abs(mref.xnai)
 
@@ -228,16 +234,8 @@ def test_cli_dropin_matches_oracle_files():
         wt = open(os.path.join(d, "wholetest_x")).read()
         lst = open(os.path.join(d, "linescan_x")).read()
         assert os.path.exists(os.path.join(d, "cadist_x"))
-    want_wt = O.wholecell_text(wc_ref)
-    want_ls = O.linescan_text(ls_ref)
-    a_lines, b_lines = wt.splitlines(), want_wt.splitlines()
-    assert len(a_lines) == len(b_lines)
-    for a, b in zip(a_lines, b_lines):
-        fa, fb = a.split(" "), b.split(" ")
-        assert len(fa) == len(fb)  # same fields and the same double spaces
-        va = np.array([float(x) for x in fa if x]), np.array([float(x) for x in fb if x])
-        np.testing.assert_allclose(va[0], va[1], rtol=1e-5, atol=2e-6)
-    assert len(lst.splitlines()) == len(want_ls.splitlines())
+    assert_text_files_match(wt, O.wholecell_text(wc_ref))
+    assert_text_files_match(lst, O.linescan_text(ls_ref))
 
 
 def test_tile_sizes_agree_and_autotune_leaves_state_unchanged():

@@ -14,7 +14,7 @@ from oracle import oracle as O
 from ryr_hyperactivity_gb300.native import NativeError
 from ryr_hyperactivity_gb300.sim import Simulator
 
-from tests.gpu_helpers import ap_waveform, c1_params, variant_params
+from tests.gpu_helpers import ap_waveform, assert_text_files_match, c1_params, variant_params
 
 pytestmark = pytest.mark.gpu
 
@@ -171,4 +171,5 @@ def test_cli_protocol_builds(variant):
         lst = open(os.path.join(d, "linescan_x")).read()
     got = np.array([[float(v) for v in line.split()] for line in wt.splitlines()])
     np.testing.assert_allclose(got, wc_ref, rtol=1e-5, atol=2e-6)
-    assert len(lst.splitlines()) == len(O.linescan_text(ls_ref).splitlines())
+    assert_text_files_match(wt, O.wholecell_text(wc_ref))
+    assert_text_files_match(lst, O.linescan_text(ls_ref))
