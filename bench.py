@@ -228,6 +228,9 @@ def main():
                     help="CRUs per CTA (64, 128, 256); 0 = pick with the autotuner")
     ap.add_argument("--groups", type=int, default=0,
                     help="cell groups on concurrent streams (0 = library default)")
+    ap.add_argument("--persistent", type=int, default=0, choices=[0, 1],
+                    help="with --tile: 1 = one persistent launch per window, 0 = two "
+                         "launches per step and cell group")
     args = ap.parse_args()
     rank, world, local = _env_rank()
     if args.impl == "reference":
@@ -260,11 +263,15 @@ def main():
     for _ in range(args.warmup):
         sim.run_steps(WINDOW)
     if args.tile:
-        tile, tune_ms = args.tile, []
-    else:  # CRU-tile length for this workload (the simulation state is unchanged)
-        tile, tune_ms = sim.autotune(40)
+        sim.set_launch_shape(args.persistent, args.tile, 0, args.groups)
+        tune = []
+    else:  # launch shape for this workload (the simulation state is unchanged)
+        _, tune = sim.autotune_shapes(40)
+    shape = sim.launch_shape()
+    tile = shape["tile_crus"]
     sim.kernel_timing()  # reset
     sim.drain_wholecell_all()
+    kernels0, persistent = sim.kernel_launches()
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
@@ -275,6 +282,7 @@ def main():
         wall = time.perf_counter() - t0
     barrier()
     launches, kms = sim.kernel_timing()  # lattice updates; CUDA events on the sim's stream
+    kernels = sim.kernel_launches()[0] - kernels0
     el = kms / 1e3
     if dist is not None:
         t = torch.tensor([el], device="cuda")
@@ -303,14 +311,23 @@ def main():
                    "step": "one output window = 100 lattice updates of every cell",
                    "l2": f"state {sim.state_bytes() / 1e9:.2f} GB > 129 MB L2, no flush",
                    "parallelism": f"cells sharded, {world} GPU(s)",
-                   "tile_crus": tile, "cell_groups": sim.num_groups(),
-                   "autotune_ms_per_step": {str(t): round(m, 4) for t, m in zip((64, 128, 256), tune_ms)}},
-        "gpu_launches": 2 * launches * sim.num_groups(),  # lattice + cell update per group
+                   "launch_shape": shape,
+                   "launch": ("one persistent cooperative launch per window, %d CTAs of %d "
+                              "threads" % (sim.window_ctas(), tile) if persistent else
+                              "two launches per step and cell group, %d groups, %d-CRU tiles"
+                              % (sim.num_groups(), tile)),
+                   "autotune_ms_per_update": [
+                       {"persistent": t["persistent"], "tile": t["tile_crus"],
+                        "fewer_ctas": t["fewer_ctas"], "groups": t["cell_groups"], "ms": round(m, 4)}
+                       for t, m in tune]},
+        "gpu_launches": kernels,  # counted by the library
         "timed_wall_s": wall,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if peak else None, "traffic": traffic,
                      "bytes_per_cru_update": bpc, "kernel_ms": avg_launch_s * 1e3,
-                     "kernel_ms_is": "one lattice update of every cell: per cell group one "
+                     "kernel_ms_is": "one lattice update of every cell (lattice and whole-cell "
+                                     "updates): the window launch's time per step" if persistent
+                                     else "one lattice update of every cell: per cell group one "
                                      "step-kernel launch and one cell-update launch, the groups "
                                      "running concurrently",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peak else None},
@@ -364,6 +381,8 @@ def main():
         sb = Simulator(cells, precision="fp64", device=local, window_steps=WINDOW, track_stats=1,
                        stats_capacity=64, block_size=args.tile, cell_groups=args.groups)
         sb.run_steps(WINDOW)
+        _, tune64 = sb.autotune_shapes(10)
+        shape64 = sb.launch_shape()
         sb.kernel_timing()
         torch.cuda.synchronize()
         nwb = 2
@@ -380,6 +399,10 @@ def main():
         result["fp64_batched"] = {
             "workload": f"heterogeneous ensemble, {args.cells} cells, FP64",
             "cru_updates_per_s": vb, "cell_beats_per_s": cbb, "kernel_ms": kb / max(lb, 1),
+            "launch_shape": shape64,
+            "autotune_ms_per_update": [
+                {"persistent": t["persistent"], "tile": t["tile_crus"], "fewer_ctas": t["fewer_ctas"],
+                 "groups": t["cell_groups"], "ms": round(m, 3)} for t, m in tune64],
             "roofline": {"bound": "fp64", "hbm_achieved": ach64, "hbm_peak": peak,
                          "hbm_frac": (ach64 / peak) if peak else None,
                          "bytes_per_cru_update": bpc64,

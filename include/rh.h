@@ -60,8 +60,10 @@ extern "C" {
                                          Gaussian draw is then NaN, is redrawn up to
                                          the 200-try cap and counts 0 */
 
-#define RH_STATUS_TIMEOUT 0x20u       /* reserved for a bounded device wait that ran
-                                         out (the kernels of this build have none) */
+#define RH_STATUS_TIMEOUT 0x20u       /* a bounded device wait of the persistent
+                                         window launch ran out (rh_run_steps then
+                                         returns RH_ERR_TIMEOUT; the lattice state
+                                         is left part-way through a step) */
 
 /* Number of columns of one wholecell record and one linescan row. */
 #define RH_WHOLECELL_COLS 45
@@ -152,6 +154,16 @@ typedef struct {
                                  values per interior CRU */
   int32_t cadist_capacity;    /* cadist records kept per cell between drains
                                  (0 = 8) */
+  int32_t persistent;         /* 1 = each window of steps is one persistent
+                                 cooperative launch: every cell's lattice and
+                                 whole-cell updates, cells synchronised by
+                                 per-cell arrival counters, a queue of cell
+                                 updates and bounded device waits (tiles of 64
+                                 or 128 CRUs; other tile lengths run the 0
+                                 path); 0 (default) = two launches per step and
+                                 cell group (lattice update, then cell update),
+                                 the faster path on GB300 (rh_autotune_shapes
+                                 measures both) */
 } rh_run_opts;
 
 /* Full FP64 view of one cell's lattice state (caller-owned host arrays of
@@ -285,14 +297,54 @@ int rh_state_bytes(const rh_sim* sim, size_t* bytes);
 int rh_export_state(rh_sim* sim, void* host, size_t bytes);
 int rh_import_state(rh_sim* sim, const void* host, size_t bytes);
 
-/* CRU-tile autotuner.  The step kernel is compiled for tiles of 64, 128 and
- * 256 CRUs per CTA (each with its own register/occupancy bound).  Times
- * `steps` lattice updates of the live workload with each candidate, starting
- * every candidate from a device-side copy of the current state and restoring
- * that state afterwards (the simulation does not advance), then keeps the
- * fastest.  ms_per_step (3 entries, may be NULL) receives the timings. */
+/* CRU-tile autotuner within the simulator's launch mode.  The step kernel is
+ * compiled for tiles of 64, 128 and 256 CRUs per CTA (each with its own
+ * register/occupancy bound).  Times `steps` lattice updates of the live
+ * workload with each candidate, starting every candidate from a device-side
+ * copy of the current state and restoring that state afterwards (the
+ * simulation does not advance), then keeps the fastest.  ms_per_step (3
+ * entries, may be NULL) receives the timings.  rh_autotune_shapes searches
+ * the launch mode, CTAs per SM and cell groups as well. */
 int rh_autotune(rh_sim* sim, int32_t steps, int32_t* tile_crus, double* ms_per_step);
 int rh_tile_size(const rh_sim* sim, int32_t* tile_crus);
+
+/* How the time steps of a simulator are launched: the autotuner's search
+ * space.  The reference launches one Compute kernel of 48 CTAs of (16,7,4)
+ * threads per step (cuda_Cell_Detailed.cu:155-158, :292-295, :420); here the
+ * shape is chosen per device and workload. */
+typedef struct {
+  int32_t persistent;   /* 1 = one persistent cooperative launch per window,
+                           0 = two launches per step and cell group */
+  int32_t tile_crus;    /* CRUs (threads) per CTA: 64, 128 or 256; the
+                           persistent launch takes 64 or 128 */
+  int32_t fewer_ctas;   /* persistent launch only: 1 = one resident CTA per SM
+                           fewer than the step kernel holds, with more registers
+                           per thread (cells without build options only) */
+  int32_t cell_groups;  /* two-launch path: cell groups on concurrent streams */
+} rh_launch_shape;
+
+int rh_get_launch_shape(const rh_sim* sim, rh_launch_shape* shape);
+
+/* Switches the simulator to `shape` (state and outputs are unaffected).
+ * RH_ERR_NOTBUILT for a shape no kernel is compiled for or the device cannot
+ * run (a persistent launch with tiles of 256, or with fewer_ctas when some
+ * cell uses a build option). */
+int rh_set_launch_shape(rh_sim* sim, const rh_launch_shape* shape);
+
+/* Launch-shape autotuner.  Times `steps` lattice updates of the live
+ * workload with every candidate shape (persistent launches with tiles of 64
+ * and 128 at both CTA counts; two-launch windows with tiles of 64, 128 and
+ * 256 at 8, 16 and 24 cell groups), each from a device-side copy of the
+ * current state that is restored afterwards (the simulation does not
+ * advance), and switches to the fastest.  The choice is cached for the
+ * process by device, precision and lattice classes (the cells' interior x
+ * and y extents in steps of 16 and their CRU total): a later simulator of
+ * the same workload on the same device reuses it without timing (then
+ * *ntried = 0).  tried/ms_per_step (max_tried entries each, may be NULL)
+ * receive the candidates and their ms per lattice update of every cell. */
+int rh_autotune_shapes(rh_sim* sim, int32_t steps, rh_launch_shape* best,
+                       rh_launch_shape* tried, double* ms_per_step, int32_t max_tried,
+                       int32_t* ntried);
 
 /* Algorithmic HBM bytes moved per interior CRU per lattice update for the
  * simulator's precision (each persistent field read once, written once). */
@@ -308,6 +360,26 @@ int rh_kernel_timing(rh_sim* sim, int64_t* launches, double* ms);
 /* Number of cell groups advanced on concurrent streams (run option
  * cell_groups, capped at the number of cells). */
 int rh_num_groups(const rh_sim* sim, int32_t* groups);
+
+/* Kernel launches issued for time steps since the simulator was created:
+ * one per window with the persistent launch, two per step and cell group
+ * otherwise.  *persistent receives whether windows run as persistent
+ * launches (the run option, unless the tile length or the device rules it
+ * out); either pointer may be NULL. */
+int rh_kernel_launches(const rh_sim* sim, int64_t* launches, int32_t* persistent);
+
+/* CTAs of the persistent window launch (its grid: every CTA the device holds
+ * at once for the simulator's tile length), 0 when windows do not run
+ * persistently. */
+int rh_window_ctas(const rh_sim* sim, int32_t* ctas);
+
+/* Testing hook of the persistent launch's bounded waits: `polls` is the
+ * number of polls (about 1 us apart) after which a wait gives up (0 = the
+ * default, about 0.3 s), `target_offset` is added to the step every wait
+ * waits for (0 = normal).  An offset that no cell reaches makes every wait
+ * run out: the next rh_run_steps returns RH_ERR_TIMEOUT and the cells carry
+ * RH_STATUS_TIMEOUT, with the GPU context intact. */
+int rh_set_wait_limit(rh_sim* sim, int64_t polls, uint32_t target_offset);
 
 /* Copies the text of the last error into buf (always NUL-terminated). */
 int rh_last_error(const rh_sim* sim, char* buf, size_t n);

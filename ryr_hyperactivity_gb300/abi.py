@@ -68,6 +68,19 @@ class CellParams(C.Structure):
     ]
 
 
+class LaunchShape(C.Structure):
+    """rh_launch_shape: how a simulator's time steps are launched."""
+    _fields_ = [
+        ("persistent", C.c_int32),
+        ("tile_crus", C.c_int32),
+        ("fewer_ctas", C.c_int32),
+        ("cell_groups", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
 class RunOpts(C.Structure):
     _fields_ = [
         ("precision", C.c_int32),
@@ -83,6 +96,7 @@ class RunOpts(C.Structure):
         ("cell_groups", C.c_int32),
         ("record_cadist", C.c_int32),
         ("cadist_capacity", C.c_int32),
+        ("persistent", C.c_int32),
     ]
 
 

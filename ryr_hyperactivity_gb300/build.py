@@ -25,7 +25,7 @@ CLI = os.path.join(BIN, "cuda_Cell_Detailed")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-I", os.path.join(ROOT, "include")]
-CU_SOURCES = ["step.cu", "rh_api.cu", "mlp.cu"]
+CU_SOURCES = ["step.cu", "window.cu", "rh_api.cu", "mlp.cu"]
 
 
 def _nvcc() -> str:

@@ -145,6 +145,7 @@ struct StepArgs {
   int stats_cap;
   int out_cap;
   int lattice_only;
+  int no_output;      // steps write no output records (the autotuner's trials)
   double dt;
 };
 

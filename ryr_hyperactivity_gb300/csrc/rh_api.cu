@@ -16,6 +16,7 @@
 #include <cmath>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -77,6 +78,19 @@ struct rh_sim {
   std::vector<double> h_ring;
   // graphs keyed by (window length, output-step bitmask)
   std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
+  // persistent window launches (run option persistent): per-cell arrival and
+  // readiness words with the update queue, the wait-timeout flag, and whether
+  // a window launch can be captured in a graph on this device (else it is
+  // launched directly)
+  bool persist_ok = false;
+  bool persist_graph = true;
+  bool fewer_ctas = false;  // persistent launch at one resident CTA per SM fewer
+  CellSync* d_sync = nullptr;
+  unsigned int* d_err = nullptr;
+  unsigned int* h_err = nullptr;  // pinned
+  long long wait_limit = kDefaultWaitLimit;
+  unsigned int wait_offset = 0;
+  long long kernels = 0;  // kernel launches issued for time steps
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timing_open = false;
@@ -287,7 +301,113 @@ cudaError_t launch_one(rh_sim* s, bool out, bool lattice_only) {
   return launch_steps(s, 1, &out, lattice_only);
 }
 
+// Whether some cell uses a build option of the lattice update (perm, iso,
+// slowncxchange, another NCX form).
+bool any_options(const rh_sim* s) {
+  for (char g : s->group_opt)
+    if (g) return true;
+  return false;
+}
+
+// Bytes of the synchronisation block of a persistent window launch: the
+// per-cell words, then the update queue (head, tail and 2 * ncells slots of
+// sequence number and cell).
+size_t sync_bytes(int ncells) {
+  return sizeof(CellSync) * (size_t)ncells + sizeof(unsigned int) * (2 + 4 * (size_t)ncells);
+}
+
+// Whether windows of steps run as one persistent launch: the run option, a
+// tile length the window kernel is compiled for, and a device that can
+// launch it cooperatively.
+bool use_persist(const rh_sim* s) {
+  const int tile = s->sets[s->ts].tile;
+  return s->opts.persistent && s->persist_ok && (tile == 64 || tile == 128);
+}
+
+// `n` steps of every cell as one persistent launch: the synchronisation
+// block is cleared first (a memset node in a captured window).  With
+// no_output the steps write no output records (the autotuner's trials).
+cudaError_t launch_persist(rh_sim* s, int n, bool no_output) {
+  cudaError_t e = cudaMemsetAsync(s->d_sync, 0, sync_bytes(s->ncells), s->stream);
+  if (e != cudaSuccess) return e;
+  WindowCtl w{};
+  w.sync = s->d_sync;
+  w.error = s->d_err;
+  w.steps = n;
+  w.ntiles = s->sets[s->ts].ntiles;
+  w.wait_limit = s->wait_limit;
+  w.wait_offset = s->wait_offset;
+  unsigned int* q = reinterpret_cast<unsigned int*>(s->d_sync + s->ncells);
+  w.q_cap = 2 * s->ncells;
+  w.q_head = q;
+  w.q_tail = q + 1;
+  w.q_seq = q + 2;
+  w.q_cell = reinterpret_cast<int*>(q + 2 + w.q_cap);
+  const bool opt = any_options(s);
+  const int tile = s->sets[s->ts].tile;
+  if (is_mixed(s)) {
+    StepArgs<float> a = make_args(s, s->Lf, false);
+    a.no_output = no_output ? 1 : 0;
+    return launch_window<float>(a, w, opt, tile, s->fewer_ctas, s->stream);
+  }
+  StepArgs<double> a = make_args(s, s->Ld, false);
+  a.no_output = no_output ? 1 : 0;
+  return launch_window<double>(a, w, opt, tile, s->fewer_ctas, s->stream);
+}
+
+// Reads and clears the wait-timeout flag of the persistent launches (the
+// stream is synchronised first).
+int check_wait_error(rh_sim* s) {
+  if (!s->d_err) return RH_OK;
+  CK(cudaMemcpyAsync(s->h_err, s->d_err, sizeof(unsigned int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  if (*s->h_err) {
+    *s->h_err = 0;
+    CK(cudaMemsetAsync(s->d_err, 0, sizeof(unsigned int), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return fail(s, RH_ERR_TIMEOUT,
+                "a wait of the persistent window launch ran out (cells flagged "
+                "RH_STATUS_TIMEOUT); the lattice state is left part-way through a step");
+  }
+  return RH_OK;
+}
+
 bool out_step_host(double t, double dt) { return fmod(t + 0.0000001, OUTT) < dt; }
+
+// Splits the cells into `want` groups of about equal CRU count (never more
+// groups than cells), each with its own stream for the two-launch path.
+int set_groups(rh_sim* s, int want) {
+  const int ncells = s->ncells;
+  want = std::max(1, std::min(want, ncells));
+  for (cudaStream_t st : s->gstreams)
+    if (st) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : s->gevents)
+    if (ev) cudaEventDestroy(ev);
+  s->gstreams.clear();
+  s->gevents.clear();
+  int64_t total = 0;
+  for (const CellConst& c : s->hcells) total += c.n;
+  s->group_cell.assign(1, 0);
+  int64_t acc = 0;
+  for (int c = 0; c < ncells; ++c) {
+    acc += s->hcells[c].n;
+    const int g = (int)s->group_cell.size();  // next boundary index
+    if (g < want && c + 1 < ncells && acc * want >= total * g) s->group_cell.push_back(c + 1);
+  }
+  s->ngroups = (int)s->group_cell.size();
+  s->group_cell.push_back(ncells);
+  s->group_opt.assign(s->ngroups, 0);
+  for (int g = 0; g < s->ngroups; ++g)
+    for (int c = s->group_cell[g]; c < s->group_cell[g + 1]; ++c)
+      if (cell_uses_options(s->hcells[c])) s->group_opt[g] = 1;
+  if (s->ngroups > 1) {
+    s->gstreams.resize(s->ngroups);
+    s->gevents.resize(s->ngroups + 1);
+    for (auto& st : s->gstreams) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    for (auto& ev : s->gevents) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  return RH_OK;
+}
 
 int ensure_diag(rh_sim* s) {
   if (s->d_diag) return RH_OK;
@@ -317,7 +437,13 @@ int check_cell(rh_sim* s, int32_t cell) {
 // Runs `n` steps in one window: replays (or captures) the graph for this
 // window's pattern of output steps.
 int run_window(rh_sim* s, int n, const std::vector<bool>& outs) {
-  auto key = std::make_pair(n, outs);
+  const bool persist = use_persist(s);
+  if (persist && !s->persist_graph) {  // this device could not capture it: launch directly
+    CK(launch_persist(s, n, false));
+    return RH_OK;
+  }
+  // a persistent window reads its output steps on the device: one graph per length
+  auto key = persist ? std::make_pair(-n, std::vector<bool>()) : std::make_pair(n, outs);
   auto it = s->graphs.find(key);
   cudaGraphExec_t exec = nullptr;
   if (it == s->graphs.end()) {
@@ -325,12 +451,25 @@ int run_window(rh_sim* s, int n, const std::vector<bool>& outs) {
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     std::unique_ptr<bool[]> o(new bool[n]);
     for (int i = 0; i < n; ++i) o[i] = outs[i];
-    cudaError_t le = launch_steps(s, n, o.get(), false);
+    cudaError_t le = persist ? launch_persist(s, n, false) : launch_steps(s, n, o.get(), false);
     cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+    cudaError_t ie = cudaErrorUnknown;
+    if (le == cudaSuccess && ce == cudaSuccess) {
+      ie = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      g = nullptr;
+    }
+    if (persist && ie != cudaSuccess) {
+      // the cooperative launch could not be captured here: launch windows directly
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      s->persist_graph = false;
+      CK(launch_persist(s, n, false));
+      return RH_OK;
+    }
     if (le != cudaSuccess) return fail(s, RH_ERR_CUDA, "launch during capture: %s", cudaGetErrorString(le));
     if (ce != cudaSuccess) return fail(s, RH_ERR_CUDA, "capture: %s", cudaGetErrorString(ce));
-    CK(cudaGraphInstantiate(&exec, g, 0));
-    cudaGraphDestroy(g);
+    CK(ie);
     if (s->graphs.size() > 64) {  // bound the cache
       for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
       s->graphs.clear();
@@ -394,6 +533,7 @@ void rh_default_run_opts(rh_run_opts* o) {
   o->stats_capacity = 64;
   o->keep_diagnostics = 0;
   o->window_steps = 100;
+  o->persistent = 0;
 }
 
 static thread_local std::string g_create_error;
@@ -539,30 +679,8 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   CK(prepare_step_kernels());
   CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   {
-    // cell groups of about equal CRU count (never more groups than cells)
-    int want = s->opts.cell_groups > 0 ? s->opts.cell_groups : kDefaultGroups;
-    want = std::max(1, std::min(want, ncells));
-    int64_t total = 0;
-    for (const CellConst& c : s->hcells) total += c.n;
-    s->group_cell.assign(1, 0);
-    int64_t acc = 0;
-    for (int c = 0; c < ncells; ++c) {
-      acc += s->hcells[c].n;
-      const int g = (int)s->group_cell.size();  // next boundary index
-      if (g < want && c + 1 < ncells && acc * want >= total * g) s->group_cell.push_back(c + 1);
-    }
-    s->ngroups = (int)s->group_cell.size();
-    s->group_cell.push_back(ncells);
-    s->group_opt.assign(s->ngroups, 0);
-    for (int g = 0; g < s->ngroups; ++g)
-      for (int c = s->group_cell[g]; c < s->group_cell[g + 1]; ++c)
-        if (cell_uses_options(s->hcells[c])) s->group_opt[g] = 1;
-    if (s->ngroups > 1) {
-      s->gstreams.resize(s->ngroups);
-      s->gevents.resize(s->ngroups + 1);
-      for (auto& st : s->gstreams) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-      for (auto& ev : s->gevents) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    }
+    int r = set_groups(s, s->opts.cell_groups > 0 ? s->opts.cell_groups : kDefaultGroups);
+    if (r) return r;
   }
   CK(cudaEventCreate(&s->ev0));
   CK(cudaEventCreate(&s->ev1));
@@ -586,6 +704,18 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
                        cudaMemcpyHostToDevice, s->stream));
   }
   CK(cudaMalloc(&s->d_partials, sizeof(double) * P_COUNT * (size_t)max_tiles));
+  CK(cudaMalloc(&s->d_sync, sync_bytes(ncells)));
+  CK(cudaMalloc(&s->d_err, sizeof(unsigned int)));
+  CK(cudaMemsetAsync(s->d_err, 0, sizeof(unsigned int), s->stream));
+  CK(cudaMallocHost(&s->h_err, sizeof(unsigned int)));
+  *s->h_err = 0;
+  {  // can this device run the persistent window kernel (cooperatively)?
+    int ctas = 0;
+    const cudaError_t we = is_mixed(s) ? window_grid<float>(128, false, false, &ctas)
+                                       : window_grid<double>(128, false, false, &ctas);
+    s->persist_ok = we == cudaSuccess && ctas > 0;
+    if (we != cudaSuccess) cudaGetLastError();
+  }
   CK(cudaMalloc(&s->d_out_wc, sizeof(double) * RH_WHOLECELL_COLS * (size_t)ncells *
                                   s->opts.output_capacity));
   if (s->opts.record_linescan)  // the reference's outputlinescan switch (:46, :967)
@@ -647,6 +777,9 @@ int rh_destroy(rh_sim* s) {
   }
   cudaFree(s->d_dyn);
   cudaFree(s->d_partials);
+  cudaFree(s->d_sync);
+  cudaFree(s->d_err);
+  if (s->h_err) cudaFreeHost(s->h_err);
   cudaFree(s->d_out_wc);
   cudaFree(s->d_out_ls);
   cudaFree(s->d_out_cd);
@@ -703,23 +836,25 @@ int rh_run_steps(rh_sim* s, int64_t nsteps) {
     }
     if (k == 0) break;
     int r;
+    const bool persist = use_persist(s);
     if (k == W) {
       r = run_window(s, k, outs);
     } else {
       r = RH_OK;
       std::unique_ptr<bool[]> o(new bool[k]);
       for (int i = 0; i < k; ++i) o[i] = outs[i];
-      cudaError_t e = launch_steps(s, k, o.get(), false);
+      cudaError_t e = persist ? launch_persist(s, k, false) : launch_steps(s, k, o.get(), false);
       if (e != cudaSuccess) return fail(s, RH_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
     }
     if (r) return r;
+    s->kernels += persist ? 1 : 2LL * s->ngroups * k;
     nlaunch += k;
     done += k;
   }
   timing_end(s, nlaunch);
   CK(cudaStreamSynchronize(s->stream));
   CK(cudaGetLastError());
-  return RH_OK;
+  return check_wait_error(s);
 }
 
 int rh_run_to_end(rh_sim* s) {
@@ -1329,21 +1464,28 @@ int rh_autotune(rh_sim* s, int32_t steps, int32_t* tile, double* ms_per_step) {
     cudaMemcpyAsync(s->arena, bk, s->arena_bytes, cudaMemcpyDeviceToDevice, s->stream);
     cudaMemcpyAsync(s->d_dyn, bk + s->arena_bytes, dyn_bytes, cudaMemcpyDeviceToDevice, s->stream);
     cudaEventRecord(e0, s->stream);
-    for (int i = 0; i < steps; ++i) {
-      // the output-free kernel variant: the trial steps write no records, so
-      // records still waiting in the output rings are never overwritten (one
-      // step in 100 is an output step; its extra stores do not move the choice)
-      cudaError_t e = launch_one(s, false, false);
-      if (e != cudaSuccess) {
-        rc = fail(s, RH_ERR_CUDA, "autotune launch: %s", cudaGetErrorString(e));
-        break;
+    // the trial steps write no output records, so records still waiting in
+    // the output rings are never overwritten (one step in 100 is an output
+    // step; its extra stores do not move the choice)
+    if (use_persist(s)) {  // one persistent launch of `steps` steps
+      cudaError_t e = launch_persist(s, steps, true);
+      if (e != cudaSuccess) rc = fail(s, RH_ERR_CUDA, "autotune launch: %s", cudaGetErrorString(e));
+    } else {
+      for (int i = 0; i < steps; ++i) {  // the output-free kernel variant
+        cudaError_t e = launch_one(s, false, false);
+        if (e != cudaSuccess) {
+          rc = fail(s, RH_ERR_CUDA, "autotune launch: %s", cudaGetErrorString(e));
+          break;
+        }
       }
     }
+    if (rc != RH_OK) break;
     cudaEventRecord(e1, s->stream);
     if (cudaEventSynchronize(e1) != cudaSuccess) {
       rc = fail(s, RH_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
       break;
     }
+    if ((rc = check_wait_error(s)) != RH_OK) break;
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     double per = ms / steps;
@@ -1369,6 +1511,178 @@ int rh_autotune(rh_sim* s, int32_t steps, int32_t* tile, double* ms_per_step) {
   if (tile) *tile = s->sets[s->ts].tile;
   CK(cudaGetLastError());
   return rc;
+}
+
+int rh_get_launch_shape(const rh_sim* s, rh_launch_shape* shape) {
+  if (!s || !shape) return RH_ERR_ARG;
+  shape->persistent = use_persist(s) ? 1 : 0;
+  shape->tile_crus = s->sets[s->ts].tile;
+  shape->fewer_ctas = (shape->persistent && s->fewer_ctas) ? 1 : 0;
+  shape->cell_groups = s->ngroups;
+  return RH_OK;
+}
+
+int rh_set_launch_shape(rh_sim* s, const rh_launch_shape* shape) {
+  if (!s || !shape) return RH_ERR_ARG;
+  int k = -1;
+  for (int i = 0; i < kNumTileSizes; ++i)
+    if (kTileSizes[i] == shape->tile_crus) k = i;
+  if (k < 0) return fail(s, RH_ERR_NOTBUILT, "no kernel for tiles of %d CRUs", shape->tile_crus);
+  if (shape->persistent) {
+    if (!s->persist_ok)
+      return fail(s, RH_ERR_NOTBUILT, "this device cannot run the persistent launch");
+    if (shape->tile_crus != 64 && shape->tile_crus != 128)
+      return fail(s, RH_ERR_NOTBUILT, "the persistent launch takes tiles of 64 or 128 CRUs");
+    if (shape->fewer_ctas && any_options(s))
+      return fail(s, RH_ERR_NOTBUILT, "fewer_ctas is compiled for cells without build options");
+  }
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  s->ts = k;
+  s->hcells = s->sets[k].hcells;
+  s->opts.persistent = shape->persistent ? 1 : 0;
+  s->fewer_ctas = shape->persistent && shape->fewer_ctas;
+  if (!shape->persistent && shape->cell_groups > 0 && shape->cell_groups != s->ngroups) {
+    int r = set_groups(s, shape->cell_groups);
+    if (r) return r;
+  }
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+  return RH_OK;
+}
+
+namespace {
+
+// Process-wide cache of rh_autotune_shapes' choices, by device, precision
+// and lattice classes.
+std::mutex g_shape_mu;
+std::map<std::string, rh_launch_shape> g_shape_cache;
+
+std::string workload_key(const rh_sim* s) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, s->device);
+  std::map<std::pair<int, int>, int> classes;  // (lx / 16, ly / 16) -> cells
+  long long crus = 0;
+  for (const CellConst& c : s->hcells) {
+    classes[{c.lx / 16, c.ly / 16}] += 1;
+    crus += c.n;
+  }
+  std::string k = std::string(prop.name) + "|sm" + std::to_string(prop.multiProcessorCount) +
+                  "|p" + std::to_string(s->opts.precision) + "|opt" +
+                  std::to_string(any_options(s) ? 1 : 0) + "|n" + std::to_string(crus);
+  for (const auto& kv : classes)
+    k += "|" + std::to_string(kv.first.first) + "," + std::to_string(kv.first.second) + ":" +
+         std::to_string(kv.second);
+  return k;
+}
+
+}  // namespace
+
+int rh_autotune_shapes(rh_sim* s, int32_t steps, rh_launch_shape* best,
+                       rh_launch_shape* tried, double* ms_per_step, int32_t max_tried,
+                       int32_t* ntried) {
+  if (!s || steps <= 0 || max_tried < 0) return RH_ERR_ARG;
+  if (ntried) *ntried = 0;
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  const std::string key = workload_key(s);
+  {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    auto it = g_shape_cache.find(key);
+    if (it != g_shape_cache.end()) {
+      const rh_launch_shape cached = it->second;
+      int r = rh_set_launch_shape(s, &cached);
+      if (r == RH_OK && best) *best = cached;
+      return r;
+    }
+  }
+  // candidates
+  std::vector<rh_launch_shape> cand;
+  if (s->persist_ok)
+    for (int tile : {64, 128})
+      for (int fewer = 0; fewer < (any_options(s) ? 1 : 2); ++fewer)
+        cand.push_back(rh_launch_shape{1, tile, fewer, 0});
+  for (int tile : {64, 128, 256})
+    for (int g : {8, 16, 24})
+      if (g <= s->ncells || g == 8) cand.push_back(rh_launch_shape{0, tile, 0, std::min(g, s->ncells)});
+  rh_launch_shape orig{};
+  rh_get_launch_shape(s, &orig);
+  // save the state on the device; every candidate starts from it
+  const size_t dyn_bytes = sizeof(CellDyn) * (size_t)s->ncells;
+  void* backup = nullptr;
+  if (cudaMalloc(&backup, s->arena_bytes + dyn_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(s, RH_ERR_NOMEM, "autotune: no room for a state copy");
+  }
+  char* bk = reinterpret_cast<char*>(backup);
+  CK(cudaMemcpyAsync(bk, s->arena, s->arena_bytes, cudaMemcpyDeviceToDevice, s->stream));
+  CK(cudaMemcpyAsync(bk + s->arena_bytes, s->d_dyn, dyn_bytes, cudaMemcpyDeviceToDevice, s->stream));
+  const std::vector<double> t0 = s->t_host;
+  const std::vector<char> a0 = s->active_host;
+  auto restore = [&]() {
+    cudaMemcpyAsync(s->arena, bk, s->arena_bytes, cudaMemcpyDeviceToDevice, s->stream);
+    cudaMemcpyAsync(s->d_dyn, bk + s->arena_bytes, dyn_bytes, cudaMemcpyDeviceToDevice, s->stream);
+  };
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  // the trial steps write no output records (see rh_autotune)
+  auto trial = [&](int n) -> cudaError_t {
+    if (use_persist(s)) return launch_persist(s, n, true);
+    for (int i = 0; i < n; ++i) {
+      cudaError_t e = launch_one(s, false, false);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
+  int rc = RH_OK, nt = 0;
+  double best_ms = 1e300;
+  rh_launch_shape win = orig;
+  for (const rh_launch_shape& c : cand) {
+    if (rh_set_launch_shape(s, &c) != RH_OK) continue;
+    restore();
+    cudaError_t e = trial(std::max(1, steps / 4));  // first launches of this shape, untimed
+    restore();
+    cudaEventRecord(e0, s->stream);
+    if (e == cudaSuccess) e = trial(steps);
+    cudaEventRecord(e1, s->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      rc = fail(s, RH_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+      break;
+    }
+    if ((rc = check_wait_error(s)) != RH_OK) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double per = ms / steps;
+    if (nt < max_tried) {
+      if (tried) tried[nt] = c;
+      if (ms_per_step) ms_per_step[nt] = per;
+    }
+    ++nt;
+    if (per < best_ms) {
+      best_ms = per;
+      win = c;
+    }
+  }
+  restore();
+  cudaStreamSynchronize(s->stream);
+  cudaFree(backup);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->t_host = t0;
+  s->active_host = a0;
+  if (ntried) *ntried = std::min(nt, max_tried);
+  const int r = rh_set_launch_shape(s, rc == RH_OK ? &win : &orig);
+  if (rc != RH_OK) return rc;
+  if (r != RH_OK) return r;
+  {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    g_shape_cache[key] = win;
+  }
+  if (best) *best = win;
+  CK(cudaGetLastError());
+  return RH_OK;
 }
 
 int rh_bytes_per_cru_step(const rh_sim* s, double* bytes) {
@@ -1401,6 +1715,36 @@ int rh_kernel_timing(rh_sim* s, int64_t* launches, double* ms) {
 int rh_num_groups(const rh_sim* s, int32_t* groups) {
   if (!s || !groups) return RH_ERR_ARG;
   *groups = s->ngroups;
+  return RH_OK;
+}
+
+int rh_kernel_launches(const rh_sim* s, int64_t* launches, int32_t* persistent) {
+  if (!s) return RH_ERR_ARG;
+  if (launches) *launches = s->kernels;
+  if (persistent) *persistent = use_persist(s) ? 1 : 0;
+  return RH_OK;
+}
+
+int rh_window_ctas(const rh_sim* s, int32_t* ctas) {
+  if (!s || !ctas) return RH_ERR_ARG;
+  *ctas = 0;
+  if (!use_persist(s)) return RH_OK;
+  int g = 0;
+  const bool opt = any_options(s);
+  const int tile = s->sets[s->ts].tile;
+  cudaError_t e = is_mixed(s) ? window_grid<float>(tile, opt, s->fewer_ctas, &g)
+                              : window_grid<double>(tile, opt, s->fewer_ctas, &g);
+  if (e != cudaSuccess) return RH_ERR_CUDA;
+  *ctas = std::min(g, s->sets[s->ts].ntiles);
+  return RH_OK;
+}
+
+int rh_set_wait_limit(rh_sim* s, int64_t polls, uint32_t target_offset) {
+  if (!s || polls < 0) return RH_ERR_ARG;
+  s->wait_limit = polls == 0 ? kDefaultWaitLimit : polls;
+  s->wait_offset = target_offset;
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);  // launch arguments changed
+  s->graphs.clear();
   return RH_OK;
 }
 

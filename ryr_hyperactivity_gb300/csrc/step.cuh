@@ -39,6 +39,53 @@ struct InitValues {
   uint32_t lcc_lo, lcc_hi;
 };
 
+// Synchronisation words of one cell inside a persistent window launch,
+// zeroed before each launch.
+struct CellSync {
+  unsigned int arrive;  // tiles of this launch that have finished (all steps)
+  unsigned int ready;   // steps of this launch whose cell update is published
+};
+// `ready` of a cell that finished its protocol: every later wait passes and
+// its tiles are skipped.
+constexpr unsigned int kReadyDone = 0x7fffffffu;
+
+// Control block of a persistent window launch (window_kernel).
+struct WindowCtl {
+  CellSync* sync;          // [ncells]
+  unsigned int* error;     // set when a wait gave up
+  int steps;               // time steps of this launch
+  int ntiles;              // tiles of the tile table
+  long long wait_limit;    // polls before a wait gives up
+  unsigned int wait_offset;  // added to every readiness target; 0 (a test sets a
+                             // target that is never published)
+  // queue of cells whose step has every arrival in and awaits its update:
+  // q_cap slots of (sequence number, cell), consumed in order
+  unsigned int* q_head;
+  unsigned int* q_tail;
+  unsigned int* q_seq;
+  int* q_cell;
+  int q_cap;
+};
+
+// Default poll limit of a wait: about 0.3 s (a poll is an L2 round trip and a
+// short sleep), far above the longest legitimate wait (a few cell updates,
+// tens of microseconds).
+constexpr long long kDefaultWaitLimit = 300000;
+
+// W time steps of every cell in one persistent cooperative launch with tiles
+// of `tile` CRUs (64 or 128): the grid is every CTA the device holds at once,
+// at the step kernel's CTAs per SM or, with fewer_ctas (plain cells only),
+// one fewer with more registers per thread.  Returns cudaErrorNotSupported
+// for a combination that is not compiled or a device that cannot launch it
+// cooperatively.
+template <class R>
+cudaError_t launch_window(const StepArgs<R>& a, const WindowCtl& w, bool opt, int tile,
+                          bool fewer_ctas, cudaStream_t st);
+
+// Resident CTAs of that persistent window kernel on this device (its grid).
+template <class R>
+cudaError_t window_grid(int tile, bool opt, bool fewer_ctas, int* ctas);
+
 // One time step with tiles of `tile` CRUs (one of kTileSizes).  `opt` selects
 // the kernel variant that handles the per-cell build options of the lattice
 // update (perm, iso, slowncxchange, NCX form); without them a cell runs the

@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from .abi import BeatStats, CellParams, Membrane, RunOpts, StateF64
+from .abi import BeatStats, CellParams, LaunchShape, Membrane, RunOpts, StateF64
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "librh.so")
 
@@ -20,7 +20,8 @@ EXPORTS = [
     "rh_drain_linescan", "rh_drain_cadist", "rh_drain_stats", "rh_cell_status", "rh_checkpoint", "rh_restore",
     "rh_bytes_per_cru_step", "rh_kernel_timing", "rh_num_groups", "rh_last_error", "rh_format_wholecell",
     "rh_format_linescan", "rh_state_bytes", "rh_export_state", "rh_import_state",
-    "rh_analyze_trace", "rh_autotune", "rh_tile_size",
+    "rh_analyze_trace", "rh_autotune", "rh_tile_size", "rh_kernel_launches", "rh_set_wait_limit",
+    "rh_window_ctas", "rh_get_launch_shape", "rh_set_launch_shape", "rh_autotune_shapes",
 ]
 
 _lib = None
@@ -74,6 +75,13 @@ def load() -> C.CDLL:
     L.rh_num_groups.argtypes = [vp, C.POINTER(C.c_int32)]
     L.rh_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), dp]
     L.rh_tile_size.argtypes = [vp, C.POINTER(C.c_int32)]
+    L.rh_kernel_launches.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
+    L.rh_set_wait_limit.argtypes = [vp, C.c_int64, C.c_uint32]
+    L.rh_window_ctas.argtypes = [vp, C.POINTER(C.c_int32)]
+    L.rh_get_launch_shape.argtypes = [vp, C.POINTER(LaunchShape)]
+    L.rh_set_launch_shape.argtypes = [vp, C.POINTER(LaunchShape)]
+    L.rh_autotune_shapes.argtypes = [vp, C.c_int32, C.POINTER(LaunchShape), C.POINTER(LaunchShape),
+                                     dp, C.c_int32, C.POINTER(C.c_int32)]
     L.rh_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
     L.rh_format_wholecell.argtypes = [dp, C.c_char_p, C.c_size_t]
     L.rh_format_linescan.argtypes = [dp, C.c_char_p, C.c_size_t]

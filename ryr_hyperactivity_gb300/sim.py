@@ -10,7 +10,7 @@ import numpy as np
 
 from . import native
 from .abi import (LINESCAN_COLS, RH_FP64, RH_MIXED, WHOLECELL_COLS, BeatStats, CellParams,
-                  HostState, Membrane, RunOpts)
+                  HostState, LaunchShape, Membrane, RunOpts)
 
 PRECISIONS = {"fp64": RH_FP64, "mixed": RH_MIXED}
 
@@ -198,6 +198,45 @@ class Simulator:
         n = C.c_int32()
         self._ck(self.L.rh_num_groups(self.h, C.byref(n)))
         return n.value
+
+    def kernel_launches(self) -> tuple[int, bool]:
+        """Kernel launches issued for time steps since creation, and whether
+        windows run as persistent launches."""
+        n, p = C.c_int64(), C.c_int32()
+        self._ck(self.L.rh_kernel_launches(self.h, C.byref(n), C.byref(p)))
+        return n.value, bool(p.value)
+
+    def window_ctas(self) -> int:
+        """CTAs of the persistent window launch (0 when windows are not persistent)."""
+        n = C.c_int32()
+        self._ck(self.L.rh_window_ctas(self.h, C.byref(n)))
+        return n.value
+
+    def set_wait_limit(self, polls: int = 0, target_offset: int = 0) -> None:
+        """Testing hook of the persistent launch's bounded waits (rh.h)."""
+        self._ck(self.L.rh_set_wait_limit(self.h, int(polls), int(target_offset)))
+
+    def launch_shape(self) -> dict:
+        sh = LaunchShape()
+        self._ck(self.L.rh_get_launch_shape(self.h, C.byref(sh)))
+        return sh.as_dict()
+
+    def set_launch_shape(self, persistent: int, tile_crus: int, fewer_ctas: int = 0,
+                         cell_groups: int = 0) -> None:
+        sh = LaunchShape(persistent, tile_crus, fewer_ctas, cell_groups)
+        self._ck(self.L.rh_set_launch_shape(self.h, C.byref(sh)))
+
+    def autotune_shapes(self, steps: int = 40) -> tuple[dict, list[tuple[dict, float]]]:
+        """Launch-shape autotuner (rh_autotune_shapes): the chosen shape and
+        every candidate timed with its ms per lattice update (empty when the
+        process-wide cache held this workload's choice)."""
+        best = LaunchShape()
+        tried = (LaunchShape * 64)()
+        ms = (C.c_double * 64)()
+        n = C.c_int32()
+        self._ck(self.L.rh_autotune_shapes(self.h, int(steps), C.byref(best), tried, ms, 64,
+                                           C.byref(n)))
+        return best.as_dict(), [(tried[i].as_dict(), float(ms[i])) for i in range(n.value)]
 
     def kernel_timing(self) -> tuple[int, float]:
         n = C.c_int64()
