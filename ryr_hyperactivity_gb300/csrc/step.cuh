@@ -42,7 +42,7 @@ struct InitValues {
 // Synchronisation words of one cell inside a persistent window launch,
 // zeroed before each launch.
 struct CellSync {
-  unsigned int arrive;  // tiles of this launch that have finished (all steps)
+  unsigned int arrive;  // tiles of the step in progress that have finished
   unsigned int ready;   // steps of this launch whose cell update is published
 };
 // `ready` of a cell that finished its protocol: every later wait passes and

@@ -13,28 +13,23 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ unsigned int ld_relaxed_u32(const unsigned int* p) {
-  unsigned int v;
-  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
 __device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-// atomic add with release semantics (device scope): publishes this CTA's
-// writes of the tile (ordered before it by the CTA barrier); the thread's
-// later loads do not wait for it
-__device__ __forceinline__ unsigned int atom_add_release_u32(unsigned int* p, unsigned int v) {
+// atomic add with acquire-release semantics at device scope: publishes this
+// CTA's writes of the tile (ordered before it by the CTA barrier) and, for
+// the thread that learns it arrived last, makes every other arrival's writes
+// visible before it queues the cell
+__device__ __forceinline__ unsigned int atom_add_acq_rel_u32(unsigned int* p, unsigned int v) {
   unsigned int old;
-  asm volatile("atom.release.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
   return old;
 }
 
 // ---- the queue of cell updates (the q_* words of WindowCtl) ----
 //
 // The CTA whose arrival completes a cell's step only enqueues the cell; the
-// update is run by a CTA that would otherwise wait, or that finds a backlog
-// at a tile boundary.  Had the last arriver run it, the update would make
+// update is run by a CTA that would otherwise wait.  Had the last arriver run it, the update would make
 // that CTA late, so it would again be the last arriver of every later cell it
 // shares tiles with: one CTA falls ~25 us per cell behind in every sweep and
 // the cells it touches become ready late (measured: 1.5 ms per step against
@@ -89,10 +84,6 @@ __device__ __noinline__ bool tile_update_output(const StepArgs<R>& a, int ti, Ti
 template <class R>
 __device__ __noinline__ void cell_update_publish(const StepArgs<R>& a, const WindowCtl& w,
                                                  int cell, int nw, double* scratch) {
-  // the arrivals are release additions to one counter: an acquiring read of
-  // it orders every arriving CTA's writes of the step before the update
-  if ((threadIdx.x & 31) == 0) (void)ld_acquire_u32(&w.sync[cell].arrive);
-  __syncwarp();
   cell_update<R, true, true>(a, cell, nw, scratch);
   __syncwarp();
   if ((threadIdx.x & 31) == 0) {
@@ -176,41 +167,22 @@ __device__ __noinline__ bool drain_updates(const StepArgs<R>& a, const WindowCtl
   }
 }
 
-// Arrival of a CTA's tile whose result is looked at later: the CTA whose
-// arrival completes the cell's step queues the cell.  Resolved before the CTA
-// waits for anything or takes an update (a wait must never hold back an
-// arrival) and otherwise after its next tile, so that the atomic's round
-// trip overlaps that tile.
-struct PendingArrival {
-  int cell;             // -1: none
-  unsigned int prev;    // the counter before this arrival
-  unsigned int target;  // the count at which the step is complete
-};
-
-__device__ __forceinline__ void resolve_arrival(const WindowCtl& w, PendingArrival& pa) {
-  if (pa.cell >= 0 && pa.prev + 1u == pa.target) enqueue_update(w, pa.cell);
-  pa.cell = -1;
-}
-
 // Persistent lattice + cell update of every active cell for w.steps time
 // steps in one launch (all CTAs resident: a cooperative launch).  CTA k takes
 // tiles k, k + G, k + 2G ... of the tile table, which is ordered by cell, so
 // each CTA sweeps the cells in the same order once per step and a cell's
 // tiles finish close together in every sweep.  Per tile and step:
-//   1. warp 0 makes sure the cell's update of the previous step is published
-//      (sync[cell].ready counts the cell's completed steps): one acquiring
-//      read per lane checks 32 tiles at once, and a tile found not ready
-//      waits in wait_or_help, running queued updates of other cells meanwhile;
+//   1. warp 0 waits until the cell's update of the previous step is published
+//      (sync[cell].ready counts the cell's completed steps), running queued
+//      updates of other cells meanwhile (wait_or_help);
 //   2. the CTA updates the tile (tile_update, the same code as step_kernel);
-//   3. thread 0 adds one arrival to the cell's counter (release); the CTA
-//      whose arrival completes the step queues the cell for its whole-cell
-//      update (cell_update, the same code as cell_kernel), which a CTA that
-//      would otherwise wait, or that finds a backlog of queued cells at a
-//      tile boundary, then runs and publishes.
+//   3. thread 0 adds one arrival for the cell; the CTA that arrives last
+//      queues the cell for its whole-cell update (cell_update, the same code
+//      as cell_kernel), which a waiting CTA then runs and publishes.
 // Each CTA finishes every tile of step i before any tile of step i + 1, an
-// update depends only on arrivals of its own step, every arrival is queued
-// before its CTA waits, and every waiting CTA runs queued updates, so the
-// waits cannot form a cycle; every wait is bounded all the same.
+// update depends only on arrivals of its own step, and every waiting CTA
+// runs queued updates, so the waits cannot form a cycle; every wait is
+// bounded all the same.
 //
 // MINB is the number of resident CTAs per SM the registers are bounded for:
 // the step kernel's count, or one less, which gives each thread more
@@ -225,62 +197,20 @@ __global__ void __launch_bounds__(B, MINB) window_kernel(StepArgs<R> a, WindowCt
   __shared__ int s_go[2];
   extern __shared__ __align__(16) unsigned char dsm[];
   constexpr int NW = B / 32;
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x;
   if (tid == 0) {
     s_a = a;
     s_w = w;
   }
   __syncthreads();
-  const int G = gridDim.x;
-  const int mine = (w.ntiles - (int)blockIdx.x + G - 1) / G;  // tiles of this CTA per step
-  // the backlog of queued cells above which a CTA at a tile boundary takes one
-  const unsigned int backlog = (unsigned int)max(8, w.q_cap / 16);
-  PendingArrival pa{-1, 0u, 0u};  // thread 0's
   int k = 0;  // double-buffered flag: a slow thread may still read the previous one
   for (int i = 0; i < w.steps; ++i) {
-    const unsigned int target = (unsigned int)i + w.wait_offset;
-    unsigned int ready_mask = 0u, skip_mask = 0u;  // warp 0's view of the next 32 tiles
-    for (int m = 0; m < mine; ++m, k ^= 1) {
-      const int ti = (int)blockIdx.x + m * G;
+    for (int ti = blockIdx.x; ti < w.ntiles; ti += gridDim.x, k ^= 1) {
       const int cell = __ldg(&a.tiles[ti].x);
       CellDyn* dyn = a.dyn + cell;
       if (tid < 32) {
-        if ((m & 31) == 0) {  // one acquiring read per lane for the next 32 tiles
-          bool ok = false, fin = false;
-          const int mj = m + lane;
-          if (mj < mine) {
-            const int cj = __ldg(&a.tiles[(int)blockIdx.x + mj * G].x);
-            const unsigned int r = ld_acquire_u32(&w.sync[cj].ready);
-            ok = r >= target;
-            fin = r == kReadyDone;
-          }
-          ready_mask = __ballot_sync(0xffffffffu, ok);
-          skip_mask = __ballot_sync(0xffffffffu, fin);
-        }
-        int go;
-        const unsigned int bit = 1u << (m & 31);
-        if (ready_mask & bit) {
-          go = (skip_mask & bit) ? 0 : 1;
-        } else {
-          if (lane == 0) resolve_arrival(w, pa);  // never wait with an arrival held back
-          __syncwarp();
-          go = wait_or_help<R>(s_a, s_w, cell, target, NW, scratch);
-        }
-        // a backlog of queued cells: this CTA takes one at its tile boundary
-        int steal = 0;
-        if (lane == 0 && go > 0 &&
-            ld_relaxed_u32(w.q_tail) - ld_relaxed_u32(w.q_head) > backlog) {
-          resolve_arrival(w, pa);
-          steal = 1;
-        }
-        steal = __shfl_sync(0xffffffffu, steal, 0);
-        if (steal) {
-          int u = lane == 0 ? try_dequeue(w) : 0;
-          u = __shfl_sync(0xffffffffu, u, 0);
-          if (u >= 0) cell_update_publish<R>(s_a, s_w, u, NW, scratch);
-          if (u == -2) go = -1;
-        }
-        if (lane == 0) s_go[k] = go;
+        const int go = wait_or_help<R>(s_a, s_w, cell, (unsigned int)i + w.wait_offset, NW, scratch);
+        if (tid == 0) s_go[k] = go;
       }
       __syncthreads();
       const int go = s_go[k];
@@ -290,18 +220,15 @@ __global__ void __launch_bounds__(B, MINB) window_kernel(StepArgs<R> a, WindowCt
       const bool did = out ? tile_update_output<R, B, OPT>(s_a, ti, sh, sk, dsm)
                            : tile_update<R, false, B, OPT>(a, ti, sh, sk, dsm);
       __syncthreads();  // every warp's sums and writes of this tile are issued
-      if (tid == 0) {
-        resolve_arrival(w, pa);  // the previous tile's, long returned by now
-        if (did) {
-          pa.cell = cell;
-          pa.target = (unsigned int)(i + 1) * (unsigned int)sh.tile_count;
-          pa.prev = atom_add_release_u32(&w.sync[cell].arrive, 1u);
+      if (tid == 0 && did) {
+        const unsigned int prev = atom_add_acq_rel_u32(&w.sync[cell].arrive, 1u);
+        if (prev + 1u == (unsigned int)sh.tile_count) {  // every arrival of this step is in
+          w.sync[cell].arrive = 0u;
+          enqueue_update(w, cell);
         }
       }
     }
   }
-  if (tid == 0) resolve_arrival(w, pa);
-  __syncwarp();
   if (tid < 32) drain_updates<R>(s_a, s_w, NW, scratch);
 }
 

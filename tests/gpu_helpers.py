@@ -150,3 +150,32 @@ def flux_errors(got: HostState, ref: HostState, mask=None):
         out[f] = float(np.max(np.abs(g - r))) / scale if r.size else 0.0
     return out
 
+
+
+def step_errors(got: HostState, ref: HostState, before: HostState, mask=None, fields=None):
+    """Per-field error of a one-step FP32 update against the FP64 oracle,
+    relative to the larger of each value before and after the step.  An FP32
+    update x + dx rounds at the scale of max(|x|, |dx|): where a concentration
+    falls by orders of magnitude within one step (the dyadic space emptying
+    once release stops), its error relative to the small new value says
+    nothing about the arithmetic.  Returns {field: (scaled error, fraction of
+    values whose plain relative error exceeds 1e-5)}."""
+    n = ref.n
+    out = {}
+    for f in fields or FLOAT_FIELDS:
+        g, r, b = got[f], ref[f], before[f]
+        if g.size == 8 * n:
+            g, r, b = g.reshape(8, n), r.reshape(8, n), b.reshape(8, n)
+            if mask is not None:
+                g, r, b = g[:, mask], r[:, mask], b[:, mask]
+        elif mask is not None:
+            g, r, b = g[mask], r[mask], b[mask]
+        if r.size == 0:
+            out[f] = (0.0, 0.0)
+            continue
+        floor = 1e-9 * max(float(np.max(np.abs(r))), 1e-300)
+        d = np.abs(g - r)
+        scaled = d / np.maximum(np.maximum(np.abs(r), np.abs(b)), floor)
+        plain = d / np.maximum(np.abs(r), floor)
+        out[f] = (float(scaled.max()), float((plain > 1e-5).mean()))
+    return out
