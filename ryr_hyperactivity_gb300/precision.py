@@ -7,10 +7,10 @@ mixed run against the FP64 run, and per parameter point the agreement of the
 ensemble statistics (mean with its 95% confidence interval in each precision).
 
     python -m ryr_hyperactivity_gb300.precision [--points 4] [--seeds 64]
-        [--nx 20 --ny 10 --nz 6] [--beats 3] [--out report.md]
+        [--nx 20 --ny 10 --nz 6] [--beats 3] [--pcl-max 1500] [--out report.md]
 
 Parameter points follow the heterogeneous ensemble (RyR-hyperactive base,
-Ku2 ~ U[1,3], IKr scale ~ U[0,1], PCL ~ U[500,1500] ms); every seed of a
+Ku2 ~ U[1,3], IKr scale ~ U[0,1], PCL ~ U[500, pcl_max] ms); every seed of a
 point is one cell with its own Philox key (seed, cell id).  Only the paced
 beats are simulated (not the 2100 ms tail of the protocol).
 """
@@ -35,11 +35,11 @@ BEAT_STATS = ["apd90_ms", "ci_peak", "sr_load", "sparks", "ead"]
 
 
 def ensemble(points: int, seeds: int, nx: int, ny: int, nz: int, beats: int,
-             param_seed: int = 2024):
+             param_seed: int = 2024, pcl_max: float = 1500.0):
     rng = np.random.default_rng(param_seed)
     ku2 = rng.uniform(1.0, 3.0, points)
     ikr = rng.uniform(0.0, 1.0, points)
-    pcl = rng.uniform(500.0, 1500.0, points)
+    pcl = rng.uniform(500.0, pcl_max, points)
     cells, meta = [], []
     for p in range(points):
         for s in range(seeds):
@@ -100,6 +100,31 @@ def beat_table(stats, meta, points, first_beat: int = 1):
     return out
 
 
+def beat_pair_errors(s64, smx, first_beat: int = 1):
+    """Per-beat errors of the mixed run against the FP64 run of the same cell
+    and beat (identical Philox streams): |dAPD90| over the beats where both
+    repolarised, and the fraction of beats whose EAD flag differs."""
+    dapd, ead_diff, ead_any, n = [], 0, 0, 0
+    for a, b in zip(s64, smx):
+        bb = {r["beat"]: r for r in b}
+        for r in a:
+            if r["beat"] < first_beat or r["beat"] not in bb:
+                continue
+            q = bb[r["beat"]]
+            n += 1
+            if r["apd90_ms"] >= 0 and q["apd90_ms"] >= 0:
+                dapd.append(abs(q["apd90_ms"] - r["apd90_ms"]))
+            ead_diff += int(bool(r["ead"]) != bool(q["ead"]))
+            ead_any += int(bool(r["ead"]) or bool(q["ead"]))
+    dapd = np.array(dapd)
+    return dict(beats=n,
+                apd90_abs_median=float(np.median(dapd)) if len(dapd) else float("nan"),
+                apd90_abs_p95=float(np.quantile(dapd, 0.95)) if len(dapd) else float("nan"),
+                apd90_abs_max=float(dapd.max()) if len(dapd) else float("nan"),
+                ead_flag_differs=ead_diff / n if n else float("nan"),
+                ead_beats_either=ead_any)
+
+
 def trace_errors(r64, rmx):
     """Per cell: max |dV| in the first 100 ms after the first stimulus and
     over the run, time of first |dV| > 1 mV, median relative errors of the
@@ -124,8 +149,8 @@ def trace_errors(r64, rmx):
     return res
 
 
-def compare(points=4, seeds=64, nx=20, ny=10, nz=6, beats=3):
-    cells, meta, pts = ensemble(points, seeds, nx, ny, nz, beats)
+def compare(points=4, seeds=64, nx=20, ny=10, nz=6, beats=3, pcl_max=1500.0):
+    cells, meta, pts = ensemble(points, seeds, nx, ny, nz, beats, pcl_max=pcl_max)
     nsteps = int(round(max(beats * p["pcl_ms"] for p in pts) / DT))
     r64, s64, t64 = run(cells, "fp64", nsteps)
     rmx, smx, tmx = run(cells, "mixed", nsteps)
@@ -144,7 +169,8 @@ def compare(points=4, seeds=64, nx=20, ny=10, nz=6, beats=3):
         agree.append(row)
     te = trace_errors(r64, rmx)
     return dict(points=pts, seeds=seeds, lattice=(nx, ny, nz), beats=beats, nsteps=nsteps,
-                seconds=dict(fp64=t64, mixed=tmx), agreement=agree, trace=te)
+                seconds=dict(fp64=t64, mixed=tmx), agreement=agree, trace=te,
+                beat_pairs=beat_pair_errors(s64, smx))
 
 
 def markdown(res) -> str:
@@ -173,6 +199,13 @@ def markdown(res) -> str:
     L.append(f"| max abs V error over the run (mV) | {q('max_dv'):.3g} | {q('max_dv', np.max):.3g} |")
     for k, name in (("rel_ci", "[Ca]i"), ("rel_cjsr", "JSR load"), ("rel_total_ca", "Total Ca")):
         L.append(f"| median relative error of {name} (records before any 1 mV V error) | {q(k):.2e} | {q(k, np.max):.2e} |")
+    bp = res.get("beat_pairs")
+    if bp:
+        L.append(f"| APD90 error per beat, same cell and beat ({bp['beats']} beats after the first; "
+                 f"median / 95th percentile, ms) | {bp['apd90_abs_median']:.3g} | "
+                 f"{bp['apd90_abs_p95']:.3g} (max {bp['apd90_abs_max']:.3g}) |")
+        L.append(f"| EAD flag differing, same cell and beat (fraction of beats; beats with an EAD "
+                 f"in either run: {bp['ead_beats_either']}) | {bp['ead_flag_differs']:.3g} | |")
     L.append("")
     L.append("The stochastic trajectories share their random numbers, so they stay together until a")
     L.append("channel draw lands on the other side of an FP32-rounded rate; after that they are two")
@@ -197,9 +230,16 @@ def main(argv=None):
     ap.add_argument("--ny", type=int, default=10)
     ap.add_argument("--nz", type=int, default=6)
     ap.add_argument("--beats", type=int, default=3)
+    ap.add_argument("--pcl-max", type=float, default=1500.0,
+                    help="upper end of the PCL draw (ms); the lower end is 500")
     ap.add_argument("--out", default="")
+    ap.add_argument("--json", default="", help="also write the raw result as JSON")
     a = ap.parse_args(argv)
-    res = compare(a.points, a.seeds, a.nx, a.ny, a.nz, a.beats)
+    res = compare(a.points, a.seeds, a.nx, a.ny, a.nz, a.beats, a.pcl_max)
+    if a.json:
+        import json
+        with open(a.json, "w") as f:
+            json.dump(res, f, default=float)
     md = markdown(res)
     if a.out:
         with open(a.out, "w") as f:
