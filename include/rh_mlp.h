@@ -72,6 +72,16 @@ int rh_mlp_last_error(const rh_mlp* m, char* buf, size_t n);
  * give wrong results.  Each
  * call writes every scratch value it reads, so nothing left by an earlier
  * call reaches the result. */
+/* Check of the network's GEMM kernels (testing aid; synchronous, default
+ * stream): C[M x N] (FP32, row-major, leading dimension ldc) = sum over k of
+ * A(m, k) B(k, n), with A(m, k) = A[m*sam + k*sak] and B(k, n) =
+ * B[k*sbk + n*sbn] BF16 device arrays and C a device array; N <= 128.
+ * tensor_cores = 1 runs the tcgen05 kernel (tensor-memory accumulator) the
+ * network uses, 0 the mma.sync kernel kept as its independent check. */
+int rh_mlp_gemm_check(const void* A, int32_t sam, int32_t sak, const void* B, int32_t sbk,
+                      int32_t sbn, float* C, int32_t ldc, int32_t M, int32_t N, int32_t K,
+                      int32_t tensor_cores);
+
 #define RH_MLP_NOALLOC_MAX_BATCH 4096
 #define RH_MLP_NOALLOC_SCRATCH_BYTES (4 * 1024 * 1024)
 int rh_mlp_forward_noalloc(const float* d_params, const float* d_x, int32_t n, float* d_y,

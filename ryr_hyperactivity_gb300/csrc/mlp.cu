@@ -5,10 +5,13 @@
 // mean), y2 = softplus(z2) (normalised APD90 variance).  Loss per sample:
 // BCE(y0, p) + (y1 - m)^2 + (y2 - s)^2, averaged over the batch.
 //
-// Every GEMM runs on the tensor cores through one hand-written kernel
-// (mma.sync m16n8k16, BF16 x BF16 -> FP32): forward Z = A W^T, backward
-// dA = dZ W and dW = dZ^T A.  Padded shapes: layer 1 K = 16 (4 inputs +
-// zeros), layer 4 N = 8 (3 outputs + zeros).
+// Every GEMM of the handle-based passes (forward Z = A W^T, backward
+// dA = dZ W and dW = dZ^T A) runs on Blackwell's 5th-generation tensor cores
+// through gemm_tc (tcgen05.mma, BF16 x BF16 -> FP32 accumulator in tensor
+// memory).  The no-allocation forward and the GEMM check keep gemm_bf16
+// (mma.sync m16n8k16), which also serves as gemm_tc's independent check.
+// Padded shapes: layer 1 K = 16 (4 inputs + zeros), layer 4 N = 8 (3
+// outputs + zeros; the tcgen05 MMA pads N to 16).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -76,6 +79,200 @@ __global__ void gemm_bf16(const __nv_bfloat16* __restrict__ A, int sam, int sak,
 #pragma unroll
   for (int q = 0; q < 4; ++q)
     if (ok[q]) *out[q] = accumulate ? *out[q] + c[q] : c[q];
+}
+
+// ---- the same GEMM on the 5th-generation tensor cores (tcgen05) ----
+//
+// One CTA of 128 threads per 128-row tile of C, every column of C (N <= 256).
+// K is staged in chunks of 128 elements: the threads copy A (128 x 128) and
+// B (N x 128, as the MMA's N x K operand) from global memory into shared
+// memory in the canonical K-major layout without swizzle (core matrices of 8
+// rows x 16 bytes), one elected thread issues eight tcgen05.mma (M = 128,
+// N = the padded width, K = 16 each) into an FP32 accumulator in tensor
+// memory and commits them to an mbarrier, and the next chunk is staged once
+// they have read shared memory.  Each warp then reads its 32 accumulator
+// rows with tcgen05.ld and writes C.  Out-of-range elements read as zero.
+// Every wait on the mbarrier is bounded: on expiry the CTA sets *err, skips
+// the rest of its MMAs and still frees its tensor memory.
+namespace tc {
+
+constexpr int kM = 128;   // rows per CTA = tensor-memory lanes
+constexpr int kKc = 128;  // K elements per staged chunk
+constexpr int kNmax = 128;
+constexpr int kSmemA = kM * kKc * 2;      // bytes
+constexpr int kSmemB = kNmax * kKc * 2;
+constexpr long long kWaitLimit = 1 << 22;  // polls of an mbarrier (a few ms)
+
+__device__ __forceinline__ uint32_t saddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor of tcgen05: start address, the byte
+// distance between core matrices adjacent along K (lbo) and along M or N
+// (sbo), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, M x N.
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+// Byte offset of element (row, k) of a staged operand with `rows` rows
+// (a multiple of 8): core matrix (row / 8, k / 8) at ((k/8) * rows/8 +
+// row/8) * 128, row % 8 at 16-byte steps, k % 8 at 2-byte steps.
+__device__ __forceinline__ uint32_t core_off(int row, int k, int rows) {
+  return (uint32_t)(((k >> 3) * (rows >> 3) + (row >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (long long it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+}  // namespace tc
+
+// C[M,N] (f32, row-major, ldc) = sum_k A(m,k) B(k,n) (+ C when accumulate),
+// with A and B addressed as in gemm_bf16; N <= 128.
+__global__ void __launch_bounds__(128, 1)
+    gemm_tc(const __nv_bfloat16* __restrict__ A, int sam, int sak,
+            const __nv_bfloat16* __restrict__ Bm, int sbk, int sbn, float* C, int ldc, int M,
+            int N, int K, int accumulate, int* err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  unsigned char* sA = smem;
+  unsigned char* sB = smem + tc::kSmemA;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * tc::kM;
+  const int Nm = (N + 15) & ~15;                 // MMA width: a multiple of 16
+  const uint32_t ncols = Nm <= 32 ? 32u : (Nm <= 64 ? 64u : 128u);  // power of two >= 32
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc::saddr(&tmem_base)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  const uint32_t idesc = tc::instr_desc(tc::kM, Nm);
+  bool ok = true;
+  const int nchunks = (K + tc::kKc - 1) / tc::kKc;
+  for (int ch = 0; ch < nchunks && ok; ++ch) {
+    const int k0 = ch * tc::kKc;
+    // stage A (128 x 128) and B (Nm x 128) as 16-byte core-matrix rows
+    for (int c = tid; c < tc::kM * (tc::kKc / 8); c += blockDim.x) {
+      const int r = c % tc::kM, kg = c / tc::kM;
+      uint32_t w[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        __nv_bfloat16 lo = __float2bfloat16(0.f), hi = lo;
+        const int m = m0 + r, k = k0 + kg * 8 + 2 * j;
+        if (m < M && k < K) lo = A[(int64_t)m * sam + (int64_t)k * sak];
+        if (m < M && k + 1 < K) hi = A[(int64_t)m * sam + (int64_t)(k + 1) * sak];
+        w[j] = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+      }
+      *reinterpret_cast<uint4*>(sA + tc::core_off(r, kg * 8, tc::kM)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    for (int c = tid; c < Nm * (tc::kKc / 8); c += blockDim.x) {
+      const int n = c % Nm, kg = c / Nm;
+      uint32_t w[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        __nv_bfloat16 lo = __float2bfloat16(0.f), hi = lo;
+        const int k = k0 + kg * 8 + 2 * j;
+        if (n < N && k < K) lo = Bm[(int64_t)k * sbk + (int64_t)n * sbn];
+        if (n < N && k + 1 < K) hi = Bm[(int64_t)(k + 1) * sbk + (int64_t)n * sbn];
+        w[j] = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+      }
+      *reinterpret_cast<uint4*>(sB + tc::core_off(n, kg * 8, Nm)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    // the staged operands become visible to the tensor core's (async) proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = tc::saddr(sA), b0 = tc::saddr(sB);
+      // K-adjacent core matrices are rows/8 * 128 bytes apart, M/N-adjacent 128
+      const uint32_t lbo_a = (tc::kM / 8) * 128, lbo_b = (uint32_t)(Nm / 8) * 128;
+#pragma unroll
+      for (int s = 0; s < tc::kKc / 16; ++s) {
+        const uint64_t ad = tc::smem_desc(a0 + (uint32_t)s * 2 * lbo_a, lbo_a, 128);
+        const uint64_t bd = tc::smem_desc(b0 + (uint32_t)s * 2 * lbo_b, lbo_b, 128);
+        const uint32_t acc = (ch > 0 || s > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              tc::saddr(&bar))
+          : "memory");
+    }
+    // every thread saw the MMAs finish (or the wait give up) before the next
+    // chunk is staged; the outcome is the same in every thread
+    ok = __syncthreads_and(tc::mbar_wait(tc::saddr(&bar), (uint32_t)(ch & 1)) ? 1 : 0) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(err, 1);
+  } else {
+    // epilogue: warp w reads accumulator rows 32w..32w+31 (its tensor-memory lanes)
+    const int row = m0 + warp * 32 + lane;
+    for (int c0 = 0; c0 < Nm; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+          "%14,%15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(ta)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int col = c0 + j;
+          if (col < N) {
+            float* o = C + (int64_t)row * ldc + col;
+            const float x = __uint_as_float(v[j]);
+            *o = accumulate ? *o + x : x;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  __syncwarp();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols)
+                 : "memory");
 }
 
 // Z += bias (per column); A = relu(Z) in BF16 (hidden layers).
@@ -188,6 +385,7 @@ struct rh_mlp {
   __nv_bfloat16 *X0, *A[3], *dZb[4];
   float *Z[4], *dA, *dZf, *y, *target, *xin, *loss;
   int64_t step = 0;
+  int* gemm_err = nullptr;  // set by a tcgen05 GEMM whose wait gave up
   std::string err;
 };
 
@@ -204,12 +402,25 @@ int ck(rh_mlp* m, cudaError_t e, const char* what) {
     if (r_) return r_;                         \
   } while (0)
 
+// Every GEMM of the network's handle-based passes runs on the tcgen05
+// kernel (the no-allocation forward keeps the mma.sync kernel).
 int gemm(rh_mlp* m, const __nv_bfloat16* A, int sam, int sak, const __nv_bfloat16* B, int sbk,
          int sbn, float* C, int ldc, int M, int N, int K, int acc) {
-  const int tiles = ((M + 15) / 16) * ((N + 7) / 8);
-  gemm_bf16<<<blocks((int64_t)tiles * 32, 128), 128, 0, m->st>>>(A, sam, sak, B, sbk, sbn, C, ldc,
-                                                                 M, N, K, acc);
+  gemm_tc<<<(M + tc::kM - 1) / tc::kM, 128, tc::kSmemA + tc::kSmemB, m->st>>>(
+      A, sam, sak, B, sbk, sbn, C, ldc, M, N, K, acc, m->gemm_err);
   return ck(m, cudaGetLastError(), "gemm");
+}
+
+// After a stream synchronisation: RH_ERR_TIMEOUT when a GEMM's wait gave up.
+int check_gemm(rh_mlp* m) {
+  int h = 0;
+  MCK(cudaMemcpy(&h, m->gemm_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    cudaMemset(m->gemm_err, 0, sizeof(int));
+    m->err = "a tensor-core GEMM's wait for its MMAs ran out";
+    return RH_ERR_TIMEOUT;
+  }
+  return RH_OK;
 }
 
 int forward(rh_mlp* m, int B) {
@@ -277,6 +488,33 @@ int run_loss(rh_mlp* m, int B, const float* xh, const float* th, float* loss_out
 
 extern "C" {
 
+int rh_mlp_gemm_check(const void* A, int32_t sam, int32_t sak, const void* B, int32_t sbk,
+                      int32_t sbn, float* C, int32_t ldc, int32_t M, int32_t N, int32_t K,
+                      int32_t tensor_cores) {
+  if (!A || !B || !C || M <= 0 || N <= 0 || N > tc::kNmax || K <= 0) return RH_ERR_ARG;
+  const __nv_bfloat16* a = static_cast<const __nv_bfloat16*>(A);
+  const __nv_bfloat16* b = static_cast<const __nv_bfloat16*>(B);
+  if (!tensor_cores) {
+    const int tiles = ((M + 15) / 16) * ((N + 7) / 8);
+    gemm_bf16<<<blocks((int64_t)tiles * 32, 128), 128>>>(a, sam, sak, b, sbk, sbn, C, ldc, M, N,
+                                                         K, 0);
+  } else {
+    int* err = nullptr;
+    if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) return RH_ERR_NOMEM;
+    cudaMemset(err, 0, sizeof(int));
+    const int smem = tc::kSmemA + tc::kSmemB;
+    cudaFuncSetAttribute(gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    gemm_tc<<<(M + tc::kM - 1) / tc::kM, 128, smem>>>(a, sam, sak, b, sbk, sbn, C, ldc, M, N, K,
+                                                      0, err);
+    int h = 0;
+    cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(err);
+    if (h) return RH_ERR_TIMEOUT;
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return RH_ERR_CUDA;
+  return RH_OK;
+}
+
 int rh_mlp_create(int32_t batch_max, int32_t device, rh_mlp** out) {
   if (!out || batch_max <= 0) return RH_ERR_ARG;
   *out = nullptr;
@@ -296,7 +534,11 @@ int rh_mlp_create(int32_t batch_max, int32_t device, rh_mlp** out) {
   int r = RH_OK;
   if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreate(&m->st) != cudaSuccess ||
       cudaMalloc(&m->P, nf * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&m->Pb, nb * sizeof(__nv_bfloat16)) != cudaSuccess) {
+      cudaMalloc(&m->Pb, nb * sizeof(__nv_bfloat16)) != cudaSuccess ||
+      cudaMalloc(&m->gemm_err, sizeof(int)) != cudaSuccess ||
+      cudaMemset(m->gemm_err, 0, sizeof(int)) != cudaSuccess ||
+      cudaFuncSetAttribute(gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           tc::kSmemA + tc::kSmemB) != cudaSuccess) {
     m->err = "allocation failed";
     r = RH_ERR_NOMEM;
   }
@@ -360,6 +602,7 @@ int rh_mlp_destroy(rh_mlp* m) {
   if (m->st) cudaStreamSynchronize(m->st);
   cudaFree(m->P);
   cudaFree(m->Pb);
+  cudaFree(m->gemm_err);
   if (m->st) cudaStreamDestroy(m->st);
   delete m;
   return RH_OK;
@@ -420,7 +663,7 @@ int rh_mlp_forward(rh_mlp* m, const float* x, int32_t n, float* y) {
                         m->st));
   }
   MCK(cudaStreamSynchronize(m->st));
-  return RH_OK;
+  return check_gemm(m);
 }
 
 int rh_mlp_gradients(rh_mlp* m, const float* x, const float* target, int32_t n, float* grads,
@@ -431,6 +674,7 @@ int rh_mlp_gradients(rh_mlp* m, const float* x, const float* target, int32_t n, 
   if ((r = backward(m, n))) return r;
   if (grads) {
     MCK(cudaStreamSynchronize(m->st));
+    if ((r = check_gemm(m))) return r;
     float* p = grads;
     for (int l = 0; l < 4; ++l) {
       const size_t nw = (size_t)m->wn[l] * m->wk[l];
@@ -460,7 +704,7 @@ int rh_mlp_train_step(rh_mlp* m, const float* x, const float* target, int32_t n,
   }
   MCK(cudaGetLastError());
   MCK(cudaStreamSynchronize(m->st));
-  return RH_OK;
+  return check_gemm(m);
 }
 
 int rh_mlp_last_error(const rh_mlp* m, char* buf, size_t n) {

@@ -92,3 +92,45 @@ def test_screening_gain_on_simulated_ensemble():
     # APD90 prediction error on unseen points
     apd_err = np.median(np.abs(pred[:, 1] * 1000.0 - stats[te, 1]))
     assert apd_err < 0.25 * np.median(stats[te, 1])
+
+
+@pytest.mark.parametrize("shape", [
+    # (M, N, K, a_k_major, b_k_major): the network's forward, dW and dA products
+    (300, 128, 128, True, True),
+    (77, 8, 16, True, True),
+    (128, 16, 1000, False, False),
+    (8, 128, 300, False, True),
+    (4096, 128, 128, True, False),
+])
+def test_tcgen05_gemm_matches_exact_product(shape):
+    """The tcgen05 GEMM (BF16 operands staged in shared memory, FP32
+    accumulator in tensor memory) against the float64 product of the same
+    BF16 values, and against the mma.sync kernel, for the operand layouts the
+    network's forward and backward passes use."""
+    import ctypes as C
+    import torch
+    from ryr_hyperactivity_gb300 import native
+    M, N, K, ak, bk = shape
+    L = native.load()
+    L.rh_mlp_gemm_check.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
+                                    C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                    C.c_int32, C.c_int32]
+    g = torch.Generator().manual_seed(M * 7 + N + K)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16)
+    B = torch.randn(K, N, generator=g).to(torch.bfloat16)
+    want = A.double().numpy() @ B.double().numpy()
+    # device layouts: A row-major (k fastest) or column-major (m fastest), B likewise
+    Ad = (A if ak else A.t().contiguous()).cuda()
+    Bd = (B.t().contiguous() if bk else B).cuda()
+    sam, sak = (K, 1) if ak else (1, M)
+    sbk, sbn = (1, K) if bk else (N, 1)
+    out = {}
+    for tcores in (1, 0):
+        Cd = torch.full((M, N), float("nan"), dtype=torch.float32, device="cuda")
+        rc = L.rh_mlp_gemm_check(Ad.data_ptr(), sam, sak, Bd.data_ptr(), sbk, sbn, Cd.data_ptr(),
+                                 N, M, N, K, tcores)
+        assert rc == 0, rc
+        out[tcores] = Cd.cpu().double().numpy()
+    scale = np.abs(want).max()
+    np.testing.assert_allclose(out[1], want, rtol=1e-5, atol=1e-5 * scale)
+    np.testing.assert_allclose(out[1], out[0], rtol=1e-5, atol=1e-5 * scale)
