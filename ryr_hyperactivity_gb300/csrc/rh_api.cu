@@ -1117,7 +1117,9 @@ int rh_set_membrane(rh_sim* s, int32_t cell, const rh_membrane* src) {
   CK(cudaSetDevice(s->device));
   CK(cudaStreamSynchronize(s->stream));
   CK(cudaMemcpy(&s->d_dyn[cell].m, src, sizeof(rh_membrane), cudaMemcpyHostToDevice));
-  CK(launch_volt_prep(s->sets[s->ts].d_cells, s->d_dyn, s->ncells, s->opts.dt_ms, s->stream));
+  // the next step's coefficients of this cell only: the others keep theirs
+  // (in mixed precision the cell update computes them in FP32)
+  CK(launch_volt_prep(s->sets[s->ts].d_cells + cell, s->d_dyn + cell, 1, s->opts.dt_ms, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   s->t_host[cell] = src->t;
   s->active_host[cell] = src->t < s->hcells[cell].tend;

@@ -159,13 +159,17 @@ class Surrogate:
 
 def simulate_points(points: np.ndarray, cells_per_point: int = 1, duration_ms: float = 6000.0,
                     lattice=(82, 18, 10), precision: str = "mixed", philox_seed: int = 7,
-                    first_id: int = 0, skip_beats: int = 1):
+                    first_id: int = 0, skip_beats: int = 1, beats_per_cell: int = 0,
+                    chunk_steps: int = 4000):
     """Runs the full stochastic model for every parameter point (Ku2, IKr scale,
     PCL, [Ca]o) and returns per point: EAD probability (fraction of recorded
     beats with an EAD), APD90 mean and variance (ms) over the recorded beats,
-    and the number of beats.  All points run in one batched simulation for
-    `duration_ms` of simulated time; the first `skip_beats` beats of each cell
-    are discarded as transient."""
+    and the number of beats.  All points run in one batched simulation for at
+    most `duration_ms` of simulated time; the first `skip_beats` beats of each
+    cell are discarded as transient.  With beats_per_cell > 0 (the shortened
+    protocol) a cell is retired, its protocol ended, as soon as it has
+    recorded skip_beats + beats_per_cell beats, so a short-PCL cell stops
+    long before a long-PCL one."""
     from .sim import Simulator
     from .workloads import HYPER
 
@@ -181,13 +185,37 @@ def simulate_points(points: np.ndarray, cells_per_point: int = 1, duration_ms: f
                                      cell_id=first_id + i * cells_per_point + r, **d))
     nsteps = int(duration_ms / 0.025)
     out = np.zeros((len(pts), 4))
+    ncell = len(cells)
+    beats = [[] for _ in range(ncell)]
     with Simulator(cells, precision=precision, window_steps=100, output_capacity=8,
                    record_linescan=0, track_stats=1, stats_capacity=64) as sim:
-        sim.run_steps(nsteps)
+        if beats_per_cell <= 0:
+            sim.run_steps(nsteps)
+            for c in range(ncell):
+                beats[c] = sim.drain_stats(c)
+        else:
+            want = skip_beats + beats_per_cell
+            live = np.ones(ncell, bool)
+            done = 0
+            while done < nsteps and live.any():
+                k = min(chunk_steps, nsteps - done)
+                sim.run_steps(k)
+                done += k
+                for c in np.flatnonzero(live):
+                    beats[c].extend(sim.drain_stats(c))
+                    if len(beats[c]) >= want:  # retire: end the cell's protocol now
+                        m = sim.get_membrane(c)
+                        m.t = 1e12
+                        sim.set_membrane(c, m)
+                        live[c] = False
+            for c in np.flatnonzero(live):
+                beats[c].extend(sim.drain_stats(c))
         for i in range(len(pts)):
             apd, ead = [], []
             for r in range(cells_per_point):
-                st = sim.drain_stats(i * cells_per_point + r)
+                st = beats[i * cells_per_point + r]
+                if beats_per_cell > 0:
+                    st = st[:skip_beats + beats_per_cell]
                 for b in st[skip_beats:]:
                     ead.append(b["ead"])
                     if b["apd90_ms"] > 0:
@@ -222,9 +250,11 @@ def _cmd_generate(a):
     rng = np.random.default_rng(a.seed)
     pts = LO + (HI - LO) * rng.random((a.points, 4))
     t0 = time.time()
-    stats = simulate_points(pts, a.cells, a.duration, tuple(a.lattice), a.precision)
+    stats = simulate_points(pts, a.cells, a.duration, tuple(a.lattice), a.precision,
+                            beats_per_cell=a.beats_per_cell)
     np.savez(a.out, points=pts, stats=stats, duration_ms=a.duration, cells_per_point=a.cells,
-             lattice=np.array(a.lattice), precision=a.precision)
+             lattice=np.array(a.lattice), precision=a.precision,
+             beats_per_cell=a.beats_per_cell)
     print(json.dumps({"points": a.points, "cells": a.cells, "seconds": time.time() - t0,
                       "ead_points": int((stats[:, 0] > 0).sum())}))
 
@@ -265,7 +295,9 @@ def verify(model: Surrogate, sweep, flagged, holdout, cap: int, threshold: float
     t0 = time.time()
     full = simulate_points(sweep[idx], int(data["cells_per_point"]), float(data["duration_ms"]),
                            tuple(int(x) for x in data["lattice"]), str(data["precision"]),
-                           philox_seed=11)
+                           philox_seed=11,
+                           beats_per_cell=int(data["beats_per_cell"]) if "beats_per_cell" in data
+                           else 0)
     pred = model.predict(normalise(sweep[idx]))
     ok = full[:, 3] > 0
     ead_true = full[:, 0] > 0
@@ -294,6 +326,9 @@ def main(argv=None):
     g.add_argument("--lattice", type=int, nargs=3, default=[82, 18, 10])
     g.add_argument("--precision", default="mixed")
     g.add_argument("--seed", type=int, default=12345)
+    g.add_argument("--beats-per-cell", type=int, default=0,
+                   help="shortened protocol: retire a cell after the first beat plus this many "
+                        "recorded beats (0 = run every cell for --duration)")
     g.add_argument("--out", required=True)
     s = sub.add_parser("screen")
     s.add_argument("--data", required=True)
