@@ -321,6 +321,10 @@ typedef struct {
                            fewer than the step kernel holds, with more registers
                            per thread (cells without build options only) */
   int32_t cell_groups;  /* two-launch path: cell groups on concurrent streams */
+  int32_t bulk_staging; /* two-launch path, FP32 lattice: 1 = a tile's own state
+                           and its stencil halo rows arrive by bulk asynchronous
+                           copies issued by one warp (completion on mbarriers),
+                           0 = every thread copies its share with cp.async */
 } rh_launch_shape;
 
 int rh_get_launch_shape(const rh_sim* sim, rh_launch_shape* shape);
@@ -334,7 +338,8 @@ int rh_set_launch_shape(rh_sim* sim, const rh_launch_shape* shape);
 /* Launch-shape autotuner.  Times `steps` lattice updates of the live
  * workload with every candidate shape (persistent launches with tiles of 64
  * and 128 at both CTA counts; two-launch windows with tiles of 64, 128 and
- * 256 at 8, 16 and 24 cell groups), each from a device-side copy of the
+ * 256 at 8, 16 and 24 cell groups, in mixed precision with either staging),
+ * each from a device-side copy of the
  * current state that is restored afterwards (the simulation does not
  * advance), and switches to the fastest.  The choice is cached for the
  * process by device, precision and lattice classes (the cells' interior x

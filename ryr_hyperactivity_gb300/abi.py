@@ -75,6 +75,7 @@ class LaunchShape(C.Structure):
         ("tile_crus", C.c_int32),
         ("fewer_ctas", C.c_int32),
         ("cell_groups", C.c_int32),
+        ("bulk_staging", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

@@ -85,6 +85,7 @@ struct rh_sim {
   bool persist_ok = false;
   bool persist_graph = true;
   bool fewer_ctas = false;  // persistent launch at one resident CTA per SM fewer
+  bool bulk = false;        // two-launch path: FP32 staging by bulk asynchronous copies
   CellSync* d_sync = nullptr;
   unsigned int* d_err = nullptr;
   unsigned int* h_err = nullptr;  // pinned
@@ -263,14 +264,14 @@ cudaError_t launch_group(rh_sim* s, int g, bool out, bool lattice_only, cudaStre
     StepArgs<float> a = make_args(s, s->Lf, lattice_only);
     a.tiles += tb;
     a.tile_base = tb;
-    if ((e = launch_step<float>(a, te - tb, out, s->group_opt[g], t.tile, st)) != cudaSuccess)
+    if ((e = launch_step<float>(a, te - tb, out, s->group_opt[g], t.tile, s->bulk, st)) != cudaSuccess)
       return e;
     return launch_cells<float>(a, c0, c1 - c0, out, t.tile, st);
   }
   StepArgs<double> a = make_args(s, s->Ld, lattice_only);
   a.tiles += tb;
   a.tile_base = tb;
-  if ((e = launch_step<double>(a, te - tb, out, s->group_opt[g], t.tile, st)) != cudaSuccess)
+  if ((e = launch_step<double>(a, te - tb, out, s->group_opt[g], t.tile, false, st)) != cudaSuccess)
     return e;
   return launch_cells<double>(a, c0, c1 - c0, out, t.tile, st);
 }
@@ -1521,6 +1522,7 @@ int rh_get_launch_shape(const rh_sim* s, rh_launch_shape* shape) {
   shape->tile_crus = s->sets[s->ts].tile;
   shape->fewer_ctas = (shape->persistent && s->fewer_ctas) ? 1 : 0;
   shape->cell_groups = s->ngroups;
+  shape->bulk_staging = (!shape->persistent && s->bulk) ? 1 : 0;
   return RH_OK;
 }
 
@@ -1537,13 +1539,18 @@ int rh_set_launch_shape(rh_sim* s, const rh_launch_shape* shape) {
       return fail(s, RH_ERR_NOTBUILT, "the persistent launch takes tiles of 64 or 128 CRUs");
     if (shape->fewer_ctas && any_options(s))
       return fail(s, RH_ERR_NOTBUILT, "fewer_ctas is compiled for cells without build options");
+    if (shape->bulk_staging)
+      return fail(s, RH_ERR_NOTBUILT, "bulk staging is compiled for the two-launch path");
   }
+  if (shape->bulk_staging && !is_mixed(s))
+    return fail(s, RH_ERR_NOTBUILT, "bulk staging is compiled for the FP32 lattice");
   CK(cudaSetDevice(s->device));
   CK(cudaStreamSynchronize(s->stream));
   s->ts = k;
   s->hcells = s->sets[k].hcells;
   s->opts.persistent = shape->persistent ? 1 : 0;
   s->fewer_ctas = shape->persistent && shape->fewer_ctas;
+  s->bulk = !shape->persistent && shape->bulk_staging;
   if (!shape->persistent && shape->cell_groups > 0 && shape->cell_groups != s->ngroups) {
     int r = set_groups(s, shape->cell_groups);
     if (r) return r;
@@ -1603,10 +1610,12 @@ int rh_autotune_shapes(rh_sim* s, int32_t steps, rh_launch_shape* best,
   if (s->persist_ok)
     for (int tile : {64, 128})
       for (int fewer = 0; fewer < (any_options(s) ? 1 : 2); ++fewer)
-        cand.push_back(rh_launch_shape{1, tile, fewer, 0});
-  for (int tile : {64, 128, 256})
-    for (int g : {8, 16, 24})
-      if (g <= s->ncells || g == 8) cand.push_back(rh_launch_shape{0, tile, 0, std::min(g, s->ncells)});
+        cand.push_back(rh_launch_shape{1, tile, fewer, 0, 0});
+  for (int bulk = 0; bulk < (is_mixed(s) ? 2 : 1); ++bulk)
+    for (int tile : {64, 128, 256})
+      for (int g : {8, 16, 24})
+        if (g <= s->ncells || g == 8)
+          cand.push_back(rh_launch_shape{0, tile, 0, std::min(g, s->ncells), bulk});
   rh_launch_shape orig{};
   rh_get_launch_shape(s, &orig);
   // save the state on the device; every candidate starts from it

@@ -90,8 +90,9 @@ cudaError_t window_grid(int tile, bool opt, bool fewer_ctas, int* ctas);
 // the kernel variant that handles the per-cell build options of the lattice
 // update (perm, iso, slowncxchange, NCX form); without them a cell runs the
 // plain variant.
+// `bulk` selects the staging by bulk asynchronous copies (FP32 only).
 template <class R>
-cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, bool opt, int tile,
+cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, bool opt, int tile, bool bulk,
                         cudaStream_t st);
 
 // The whole-cell update of cells [cell0, cell0 + ncells) after their lattice

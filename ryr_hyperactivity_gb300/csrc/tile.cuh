@@ -221,7 +221,68 @@ struct TileSmem {
   static constexpr size_t kHcs = kHz + 16 * sizeof(R) * B;  // R[dir][B]
   static constexpr size_t kHx = kHcs + 2 * sizeof(R) * B;  // V[2][4][2]
   static constexpr size_t kBytes = kStage ? kHx + 16 * sizeof(V) : 8 * kPlane;
+  // The bulk-copy staging (BULK, FP32 only) keeps the tile's own planes,
+  // scalars and integers at the offsets above and moves the halo as whole
+  // rows: each of the y and z halo planes holds B + 2 pairs (the row may
+  // start one pair before a 16-byte boundary), the cs rows of the z
+  // neighbours B + 4 values.
+  static constexpr size_t kRowV = sizeof(V) * (B + 2);
+  static constexpr size_t kRowR = sizeof(R) * (B + 4);
+  static constexpr size_t kHyB = kWin + 4 * B;
+  static constexpr size_t kHzB = kHyB + 8 * kRowV;   // V[dir][pair plane][field][B + 2]
+  static constexpr size_t kHcsB = kHzB + 16 * kRowV;  // R[dir][B + 4]
+  static constexpr size_t kHxB = kHcsB + 2 * kRowR;   // V[2][4][2]
+  static constexpr size_t kBytesBulk = kHxB + 16 * sizeof(V);
+  static_assert(kRowV % 16 == 0 && kRowR % 16 == 0 && kHyB % 16 == 0, "bulk rows 16-byte aligned");
 };
+
+// ---- bulk asynchronous copies (the tensor-memory-access engine's linear
+//      mode) into shared memory, completing on an mbarrier ----
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+// Bounded wait for the phase with parity `parity`; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+// Elements [first, first + n) of a row of `len` elements of `esz` bytes into
+// dst (dst[0] <- element first); only the part inside [0, len) moves (the
+// rest is never read).  first, n and len are multiples of 16 / esz, the row
+// and dst 16-byte aligned, so every copy starts and ends on a 16-byte
+// boundary.
+__device__ __forceinline__ void bulk_row(void* dst, const void* row, long long first, int n,
+                                         int esz, long long len, uint64_t* bar) {
+  const long long lo = first > 0 ? first : 0;
+  const long long hi = first + n < len ? first + n : len;
+  if (hi <= lo) return;
+  const uint32_t bytes = (uint32_t)((hi - lo) * esz);
+  mbar_expect_tx(bar, bytes);
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(static_cast<char*>(dst) + (lo - first) * esz)),
+      "l"(static_cast<const char*>(row) + lo * esz), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
 
 struct TileHeader {
   int lx, ly, lz, nxf, nyf, tile_count, line_y, line_z;
@@ -239,12 +300,20 @@ struct TileHeader {
 // Returns false, with no work done, when the cell has finished its protocol.
 // Per-cell state is read through L2 (__ldcg): inside the persistent window
 // kernel other CTAs write it during the launch.
-template <class R, bool OUT, int B, bool OPT>
+//
+// BULK (FP32 only) stages with bulk asynchronous copies issued by warp 0 into
+// two mbarriers (`bars`, initialised with one arrival each, phase `phase`):
+// the tile's own planes, scalars, integers and the cs of its z neighbours,
+// then the y and z halo rows; otherwise every thread issues cp.async copies
+// of its own share and of its CRU's halo.
+template <class R, bool OUT, int B, bool OPT, bool BULK = false>
 __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHeader& sh,
-                                            StepCoef<R>& sk, unsigned char* dsm) {
+                                            StepCoef<R>& sk, unsigned char* dsm,
+                                            uint64_t* bars = nullptr, uint32_t phase = 0) {
   constexpr int kBlock = B;
   using TS = TileSmem<R, B>;
   constexpr bool kStage = TS::kStage;
+  static_assert(!BULK || kStage, "bulk staging is the FP32 staging");
   using V = typename Vec2<R>::T;
   V(*s_ci2)[kBlock] = reinterpret_cast<V(*)[kBlock]>(dsm + TS::kCi);
   V(*s_cn2)[kBlock] = reinterpret_cast<V(*)[kBlock]>(dsm + TS::kCn);
@@ -267,7 +336,7 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
   // creation), so every element index, 8 sub-voxels per CRU included, is
   // below 2^32 and each address is one 32x64 multiply-add.
   const uint32_t gt0 = (uint32_t)tile.w;  // arena index of the tile's first CRU
-  if (kStage) {
+  if (kStage && !BULK) {
     // Fields updated in place do not depend on the ping-pong parity, so
     // their copies start before the cell header arrives.  16-byte chunks:
     // a pair plane holds 2 CRUs per chunk, a 4-byte plane 4.
@@ -340,8 +409,80 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
   const V* ci2 = reinterpret_cast<const V*>(L.ci[par]);
   const V* cn2 = reinterpret_cast<const V*>(L.cnsr[par]);
 
+  // ---- bulk staging: warp 0 issues whole rows ----
+  // halo row offsets: a row starts at the 16-byte boundary at or before the
+  // first neighbour, `o*` elements before it (gt0 is a multiple of 32)
+  const int oy = lx & 1, oz = lxly & 1, ocp = lxly & 3, ocm = (4 - (lxly & 3)) & 3;
+  V(*b_hy)[2][2][kBlock + 2] = reinterpret_cast<V(*)[2][2][kBlock + 2]>(dsm + TS::kHyB);
+  V(*b_hz)[4][2][kBlock + 2] = reinterpret_cast<V(*)[4][2][kBlock + 2]>(dsm + TS::kHzB);
+  R(*b_hcs)[kBlock + 4] = reinterpret_cast<R(*)[kBlock + 4]>(dsm + TS::kHcsB);
+  V(*b_hx)[4][2] = reinterpret_cast<V(*)[4][2]>(dsm + TS::kHxB);
+  if constexpr (BULK) {
+    const int lane = tid & 31;
+    if (tid < 32) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // after the last tile's reads
+      const long long S64 = (long long)S, g0 = (long long)gt0;
+      // group 1 (bars[0]): what the channel part reads
+      if (lane < 8) {  // own pair planes: ci, cnsr x 4
+        const V* f = (lane >> 2) ? cn2 : ci2;
+        const int pl = lane & 3;
+        V(*dst)[kBlock] = (lane >> 2) ? s_cn2 : s_ci2;
+        bulk_row(dst[pl], f + pl * S64, g0, cpad, 8, S64, &bars[0]);
+      } else if (lane < 16) {  // cp cjsr cjsrb ancx casar casarh casarj casarhj
+        const int k = lane - 8;
+        const R* f = k == 0 ? L.cp : k == 1 ? L.cjsr : k == 2 ? L.cjsrb : k == 3 ? L.ancx
+                   : k == 4 ? L.casar : k == 5 ? L.casarh : k == 6 ? L.casarj : L.casarhj;
+        bulk_row(s_sc[k], f, g0, cpad, 4, S64, &bars[0]);
+      } else if (lane == 16) {
+        bulk_row(s_cs, L.cs[par], g0, cpad, 4, S64, &bars[0]);
+      } else if (lane == 17) {
+        bulk_row(s_lcc, L.lcc, g0, cpad, 8, S64, &bars[0]);
+      } else if (lane == 18) {
+        bulk_row(s_ryr, L.ryr, g0, cpad, 4, S64, &bars[0]);
+      } else if (lane == 19) {
+        bulk_row(s_win, L.win, g0, cpad, 4, S64, &bars[0]);
+      } else if (lane == 20) {  // cs of the CRUs above (+z)
+        bulk_row(b_hcs[1], L.cs[par], g0 + lxly - ocp, (count + ocp + 3) & ~3, 4, S64, &bars[0]);
+      } else if (lane == 21) {  // and below (-z)
+        bulk_row(b_hcs[0], L.cs[par], g0 - lxly - ocm, (count + ocm + 3) & ~3, 4, S64, &bars[0]);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bars[0]);
+      // group 2 (bars[1]): the y and z halo rows of ci and cnsr
+      if (lane < 8) {  // y: dir 1 (+lx) planes 0, 2; dir 0 (-lx) planes 1, 3
+        const int dir = lane >> 2, j = (lane >> 1) & 1, fld = lane & 1;
+        const int pl = dir ? 2 * j : 2 * j + 1;
+        const V* f = (fld ? cn2 : ci2) + pl * S64;
+        const long long first = g0 + (dir ? lx : -lx) - oy;
+        bulk_row(b_hy[dir][j][fld], f, first, (count + oy + 1) & ~1, 8, S64, &bars[1]);
+      } else if (lane < 24) {  // z: whole pairs of the CRUs above (dir 1) and below (dir 0)
+        const int k = lane - 8, dir = k >> 3, pl = (k >> 1) & 3, fld = k & 1;
+        const V* f = (fld ? cn2 : ci2) + pl * S64;
+        const long long first = g0 + (dir ? lxly : -lxly) - oz;
+        bulk_row(b_hz[dir][pl][fld], f, first, (count + oz + 1) & ~1, 8, S64, &bars[1]);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bars[1]);
+    }
+    // the x halo: one CRU before and one after the tile (two threads)
+    if (valid) {
+      const int hx = q % lx;
+#pragma unroll
+      for (int f = 0; f < 2; ++f) {
+        const V* src = f ? cn2 : ci2;
+#pragma unroll
+        for (int pl = 0; pl < 4; ++pl) {
+          if (tid == 0 && hx > 0) cp_async8(&b_hx[0][pl][f], src + pl * S + g - 1);
+          if (tid == count - 1 && hx + 1 < lx) cp_async8(&b_hx[1][pl][f], src + pl * S + g + 1);
+        }
+      }
+    }
+    cp_async_commit();
+    if (!mbar_wait(&bars[0], phase)) atomicOr(&a.dyn[cell].status, (unsigned int)RH_STATUS_TIMEOUT);
+  }
+
   // ---- stage the tile's own sub-voxels (z-pairs) ----
-  if (kStage) {
+  if (kStage && !BULK) {
     constexpr int kTpp = kBlock / 2;
     const int c2 = tid % kTpp, h2 = tid / kTpp;
     if (2 * c2 < cpad) {
@@ -386,7 +527,7 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
     }
     cp_async_commit();       // group 2: the halo, which only its own thread reads
     cp_async_wait_group<1>();  // group 1 has landed (this thread's part of it)
-  } else {
+  } else if (!kStage) {
 #pragma unroll
     for (int p = 0; p < 4; ++p) {
       s_ci2[p][tid] = valid ? ci2[p * S + g] : splat2(R(0));
@@ -568,8 +709,8 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
       // cell's bath value, which its ghosts keep (:1603-1689 under -Dperm)
       const R cs_face = o_perm ? R(PERM_CI_BASAL) : cs0;
       R csN = cs_face, csS = cs_face;
-      if (has_zp) csN = kStage ? s_hcs[1][tid] : __ldg(cs + g + lxly);
-      if (has_zm) csS = kStage ? s_hcs[0][tid] : __ldg(cs + g - lxly);
+      if (has_zp) csN = BULK ? b_hcs[1][tid + ocp] : kStage ? s_hcs[1][tid] : __ldg(cs + g + lxly);
+      if (has_zm) csS = BULK ? b_hcs[0][tid + ocm] : kStage ? s_hcs[0][tid] : __ldg(cs + g - lxly);
       const R csdiff = (csN + csS - R(2) * cs0) * R(1.0 / TAUST);
       const R cs_const = -R(ICAGAMMA * VP / VS) * icat1 + xinaca -
                          (cs0 - ci0) * R(1.0 / TAUSI / 2.) - (cs0 - ci1) * R(1.0 / TAUSI / 2.) +
@@ -623,6 +764,9 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
     // the channel part above reads no halo; the sub-voxel part below needs
     // this thread's halo copies
     if (kStage) cp_async_wait_group<0>();
+    if constexpr (BULK) {
+      if (!mbar_wait(&bars[1], phase)) tstat |= RH_STATUS_TIMEOUT;
+    }
 
     // ---- sub-voxel diffusion, SERCA/leak, cytosolic buffers (:1305-1393) ----
     // Processed as four z-pairs p = (sub-voxels 2p, 2p+1).  Along z the pair's
@@ -670,7 +814,16 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
       const V cface = o_perm ? splat2(R(PERM_CI_BASAL)) : c;
       // z
       V czp = c, nzp = n, czm = c, nzm = n;
-      if (kStage) {
+      if (BULK) {
+        if (has_zp) {
+          czp.x = b_hz[1][p][0][tid + oz].x;
+          nzp.x = b_hz[1][p][1][tid + oz].x;
+        }
+        if (has_zm) {
+          czm.y = b_hz[0][p][0][tid + oz].y;
+          nzm.y = b_hz[0][p][1][tid + oz].y;
+        }
+      } else if (kStage) {
         if (has_zp) {
           czp.x = s_hz[1][p][0][tid];
           nzp.x = s_hz[1][p][1][tid];
@@ -709,7 +862,10 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
         V ci_ex = cface, cn_ex = n;
         const int d = by ? lx : -lx;
         if (by ? has_yp : has_ym) {
-          if (kStage) {
+          if (BULK) {
+            ci_ex = b_hy[by][p >> 1][0][tid + oy];
+            cn_ex = b_hy[by][p >> 1][1][tid + oy];
+          } else if (kStage) {
             ci_ex = s_hy[by][p >> 1][0][tid];
             cn_ex = s_hy[by][p >> 1][1][tid];
           } else if (by ? yp_in : ym_in) {
@@ -736,6 +892,9 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
           if (bx ? xp_in : xm_in) {
             ci_ex = s_ci2[px][tid + d];
             cn_ex = s_cn2[px][tid + d];
+          } else if (BULK) {
+            ci_ex = b_hx[bx][px][0];
+            cn_ex = b_hx[bx][px][1];
           } else if (kStage) {
             ci_ex = s_hx[bx][px][0];
             cn_ex = s_hx[bx][px][1];
@@ -931,6 +1090,12 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
         r[21] = (double)xinaca;
       }
     }
+  }
+
+  // every thread waits for the halo rows, so no bulk copy is still writing
+  // this CTA's shared memory when it finishes
+  if constexpr (BULK) {
+    if (!valid) mbar_wait(&bars[1], phase);
   }
 
   // ---- per-warp reduction: the per-step sums exactly (fixedsum.cuh) into

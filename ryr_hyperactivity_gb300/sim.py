@@ -222,8 +222,8 @@ class Simulator:
         return sh.as_dict()
 
     def set_launch_shape(self, persistent: int, tile_crus: int, fewer_ctas: int = 0,
-                         cell_groups: int = 0) -> None:
-        sh = LaunchShape(persistent, tile_crus, fewer_ctas, cell_groups)
+                         cell_groups: int = 0, bulk_staging: int = 0) -> None:
+        sh = LaunchShape(persistent, tile_crus, fewer_ctas, cell_groups, bulk_staging)
         self._ck(self.L.rh_set_launch_shape(self.h, C.byref(sh)))
 
     def autotune_shapes(self, steps: int = 40) -> tuple[dict, list[tuple[dict, float]]]:
