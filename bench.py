@@ -231,6 +231,9 @@ def main():
     ap.add_argument("--persistent", type=int, default=0, choices=[0, 1],
                     help="with --tile: 1 = one persistent launch per window, 0 = two "
                          "launches per step and cell group")
+    ap.add_argument("--bulk", type=int, default=0, choices=[0, 1],
+                    help="with --tile, two-launch path, mixed precision: 1 = staging by bulk "
+                         "asynchronous copies")
     args = ap.parse_args()
     rank, world, local = _env_rank()
     if args.impl == "reference":
@@ -263,7 +266,7 @@ def main():
     for _ in range(args.warmup):
         sim.run_steps(WINDOW)
     if args.tile:
-        sim.set_launch_shape(args.persistent, args.tile, 0, args.groups)
+        sim.set_launch_shape(args.persistent, args.tile, 0, args.groups, args.bulk)
         tune = []
     else:  # launch shape for this workload (the simulation state is unchanged)
         _, tune = sim.autotune_shapes(40)

@@ -92,7 +92,7 @@ def test_persistent_with_fewer_ctas_per_sm_equals_two_launch_path(precision):
     with Simulator(cells, precision=precision) as sim:
         sim.set_launch_shape(persistent=1, tile_crus=128, fewer_ctas=1)
         assert sim.launch_shape() == {"persistent": 1, "tile_crus": 128, "fewer_ctas": 1,
-                                      "cell_groups": sim.num_groups()}
+                                      "cell_groups": sim.num_groups(), "bulk_staging": 0}
         for k in chunks:
             sim.run_steps(k)
         out["membrane"] = [sim.get_membrane(c).as_dict() for c in range(2)]
@@ -110,8 +110,10 @@ def test_shape_autotuner_restores_state_and_caches_its_choice():
         a.run_steps(150)
         b.run_steps(150)
         best, tried = a.autotune_shapes(8)
-        # 4 persistent shapes; 3 tile lengths at one group count (6 cells cap it)
-        assert len(tried) == 7 and all(ms > 0 for _, ms in tried)
+        # 4 persistent shapes; 3 tile lengths at one group count (6 cells cap
+        # it), with either staging
+        assert len(tried) == 10 and all(ms > 0 for _, ms in tried)
+        assert {t["bulk_staging"] for t, _ in tried} == {0, 1}
         assert {t["persistent"] for t, _ in tried} == {0, 1}
         assert a.launch_shape()["tile_crus"] == best["tile_crus"]
         assert a.get_membrane(0).step == 150
