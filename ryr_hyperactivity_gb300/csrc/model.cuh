@@ -192,12 +192,14 @@ __device__ __forceinline__ R pow23(R x) {  // x^23 = x^16 x^4 x^2 x
 
 // ---- buffers (buffers.c:55-155) ----
 
-// Mass-action rate with the reference's saturation guard kon*c*dt > 1.
+// Mass-action rate with the reference's saturation guard kon*c*dt > 1, which
+// replaces the on-rate kon*c by 0.95/dt: the guard selects the factor, one
+// expression computes the rate.
 template <class R>
 __device__ __forceinline__ R buffer_rate(R kon, R koff, R total, R bound, R c, R dt, R rdt95) {
   R on = kon * c;
-  return (on * dt > R(1)) ? rdt95 * (total - bound) - koff * bound
-                          : on * (total - bound) - koff * bound;
+  on = (on * dt > R(1)) ? rdt95 : on;
+  return on * (total - bound) - koff * bound;
 }
 
 // ---- CSQN (subroutine_cuda.c:161-195) ----

@@ -456,7 +456,11 @@ int run_window(rh_sim* s, int n, const std::vector<bool>& outs) {
     cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
     cudaError_t ie = cudaErrorUnknown;
     if (le == cudaSuccess && ce == cudaSuccess) {
-      ie = cudaGraphInstantiate(&exec, g, 0);
+      // Per-node priorities: without this flag a graph launch runs every
+      // node at the priority of the stream it is launched into, and the
+      // cell updates' launch priority is lost (measured on the 512-cell
+      // ensemble: 0.510 against 0.520 ms per update of every cell).
+      ie = cudaGraphInstantiate(&exec, g, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(g);
       g = nullptr;
     }
@@ -1613,7 +1617,7 @@ int rh_autotune_shapes(rh_sim* s, int32_t steps, rh_launch_shape* best,
         cand.push_back(rh_launch_shape{1, tile, fewer, 0, 0});
   for (int bulk = 0; bulk < (is_mixed(s) ? 2 : 1); ++bulk)
     for (int tile : {64, 128, 256})
-      for (int g : {8, 16, 24})
+      for (int g : {8, 12, 16, 24})
         if (g <= s->ncells || g == 8)
           cand.push_back(rh_launch_shape{0, tile, 0, std::min(g, s->ncells), bulk});
   rh_launch_shape orig{};

@@ -196,8 +196,9 @@ cudaError_t launch_cells(const StepArgs<R>& a, int cell0, int ncells, bool out, 
   cfg.stream = st;
   // Programmatic serialization after the lattice launch, and the device's
   // highest launch priority: when lattice CTAs of the other groups are also
-  // waiting for an SM, the cell warps go first (measured: without the
-  // priority the early launch made the step slower).
+  // waiting for an SM, the cell warps go first.  Inside a captured window
+  // the priority holds because the window's graph is instantiated with
+  // per-node priorities.
   int prio_low = 0, prio_high = 0;
   cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
   if (e != cudaSuccess) return e;

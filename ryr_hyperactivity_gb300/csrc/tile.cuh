@@ -926,16 +926,24 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
         const V den = vadd(n2, splat2(R(KJSR_LEAK * KJSR_LEAK)));
         lk = v2(Math<R>::div(num.x, den.x), Math<R>::div(num.y, den.y));
       }
-      // cytosolic buffers (buffers.c:55-115): on*(B-b) - koff*b, with the
-      // saturation guard kon*c*dt > 1 taken on the rare slow path
+      // cytosolic buffers (buffers.c:55-115): on*(B-b) - koff*b, where the
+      // saturation guard kon*c*dt > 1 replaces on by 0.95/dt.  Myosin's
+      // guard (kon 13.8 per uM ms) trips from c = 2.9 uM on, which the
+      // sub-voxels near a releasing dyad pass in most warps of a beating
+      // cell: its on-rate is a per-half select.  The other four (kon <= 0.1,
+      // from c = 400 uM on) take the slow path.
       const V freemyo = vsub(vsub(splat2(R(BMYO)), camyo), mgmyo);
       V r_tf = vfma(vmul(splat2(R(KTFON)), c), vsub(splat2(R(BTF)), catf), vmul(splat2(R(-KTFOFF)), catf));
       V r_ts = vfma(vmul(splat2(R(KTSON)), c), vsub(splat2(R(BTS)), cats), vmul(splat2(R(-KTSOFF)), cats));
       V r_cal = vfma(vmul(splat2(R(KCALON)), c), vsub(splat2(R(BCAL)), cacal),
                      vmul(splat2(R(-KCALOFF)), cacal));
       V r_sr = vfma(vmul(splat2(R(KSRON)), c), vsub(splat2(R(BSR)), casr), vmul(splat2(R(-KSROFF)), casr));
-      V r_mc = vfma(vmul(splat2(R(KONMYOCA)), c), freemyo, vmul(splat2(R(-KOFFMYOCA)), camyo));
-      if (fmax(c.x, c.y) * R(KONMYOCA) * dt > R(1)) {  // some buffer saturates
+      V on_mc = vmul(splat2(R(KONMYOCA)), c);
+      on_mc.x = (on_mc.x * dt > R(1)) ? k.rdt95 : on_mc.x;
+      on_mc.y = (on_mc.y * dt > R(1)) ? k.rdt95 : on_mc.y;
+      const V r_mc = vfma(on_mc, freemyo, vmul(splat2(R(-KOFFMYOCA)), camyo));
+      static_assert(KTFON <= KSRON && KTSON <= KSRON && KCALON <= KSRON, "SR has the largest on-rate");
+      if (fmax(c.x, c.y) * R(KSRON) * dt > R(1)) {  // another buffer saturates
         const R cc[2] = {c.x, c.y};
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -944,15 +952,10 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
           R& ts = h ? r_ts.y : r_ts.x;
           R& cal = h ? r_cal.y : r_cal.x;
           R& sr = h ? r_sr.y : r_sr.x;
-          R& mc = h ? r_mc.y : r_mc.x;
           tf = buffer_rate<R>(R(KTFON), R(KTFOFF), R(BTF), h ? catf.y : catf.x, cv, dt, k.rdt95);
           ts = buffer_rate<R>(R(KTSON), R(KTSOFF), R(BTS), h ? cats.y : cats.x, cv, dt, k.rdt95);
           cal = buffer_rate<R>(R(KCALON), R(KCALOFF), R(BCAL), h ? cacal.y : cacal.x, cv, dt, k.rdt95);
           sr = buffer_rate<R>(R(KSRON), R(KSROFF), R(BSR), h ? casr.y : casr.x, cv, dt, k.rdt95);
-          const R fmy = h ? freemyo.y : freemyo.x;
-          const R cm = h ? camyo.y : camyo.x;
-          const R onmc = R(KONMYOCA) * cv;
-          mc = (onmc * dt > R(1)) ? k.rdt95 * fmy - R(KOFFMYOCA) * cm : onmc * fmy - R(KOFFMYOCA) * cm;
         }
       }
       V dotcn = vfma(vsub(up, lk), splat2(R(VI / VNSR)), coupn);
