@@ -184,6 +184,21 @@ __device__ __forceinline__ V vclamp0(V a) {
   return a;
 }
 
+// SERCA's (x / K)^1.787 for x >= 0 (subroutine_cuda.c:128-146), K = KI_UP
+// for the cytosol (SIDE 0) and KNSR_UP for the network SR (SIDE 1).  FP64 as
+// exp(1.787 log(x / K)); FP32 as ex2(1.787 lg2(x) - 1.787 lg2(K)), the
+// division folded into the constant (lg2(0.123) = -3.0232697793228470,
+// lg2(1700) = 10.731319031025064).
+template <int SIDE>
+__device__ __forceinline__ double serca_pow(double x) {
+  return Math<double>::powpos(x * (1.0 / (SIDE ? KNSR_UP : KI_UP)), HH_UP);
+}
+template <int SIDE>
+__device__ __forceinline__ float serca_pow(float x) {
+  constexpr double lg2k = SIDE ? 10.731319031025064 : -3.0232697793228470;
+  return ex2_approx(fmaf((float)HH_UP, __log2f(x), (float)(-HH_UP * lg2k)));
+}
+
 template <class R>
 __device__ __forceinline__ R pow23(R x) {  // x^23 = x^16 x^4 x^2 x
   R x2 = x * x, x4 = x2 * x2, x8 = x4 * x4, x16 = x8 * x8;

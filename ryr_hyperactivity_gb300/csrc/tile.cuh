@@ -854,8 +854,10 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
       }
       const V ciN = v2(c.y, has_zp ? czp.x : cface.y), cnN = v2(n.y, has_zp ? nzp.x : n.y);
       const V ciS = v2(has_zm ? czm.y : cface.x, c.x), cnS = v2(has_zm ? nzm.y : n.x, n.x);
-      // y: pair p^1
-      V ciE, cnE, ciW, cnW;
+      // y: pair p^1 of this CRU (inside) and of the CRU on the side of the
+      // pair's y bit (outside).  The stencil only sums the two differences,
+      // so they need no east/west order.
+      V ciy_in, cny_in, ciy_ex, cny_ex;
       {
         const int py = p ^ 1;
         const V ci_in = s_ci2[py][tid], cn_in = s_cn2[py][tid];
@@ -876,13 +878,13 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
             cn_ex = __ldg(cn2 + py * S + g + d);
           }
         }
-        ciE = by ? ci_ex : ci_in;
-        cnE = by ? cn_ex : cn_in;
-        ciW = by ? ci_in : ci_ex;
-        cnW = by ? cn_in : cn_ex;
+        ciy_in = ci_in;
+        cny_in = cn_in;
+        ciy_ex = ci_ex;
+        cny_ex = cn_ex;
       }
-      // x: pair p^2
-      V ciT, cnT, ciB, cnB;
+      // x: pair p^2, likewise
+      V cix_in, cnx_in, cix_ex, cnx_ex;
       {
         const int px = p ^ 2;
         const V ci_in = s_ci2[px][tid], cn_in = s_cn2[px][tid];
@@ -903,22 +905,22 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
             cn_ex = __ldg(cn2 + px * S + g + d);
           }
         }
-        ciT = bx ? ci_ex : ci_in;
-        cnT = bx ? cn_ex : cn_in;
-        ciB = bx ? ci_in : ci_ex;
-        cnB = bx ? cn_in : cn_ex;
+        cix_in = ci_in;
+        cnx_in = cn_in;
+        cix_ex = ci_ex;
+        cnx_ex = cn_ex;
       }
-      const V coupn = vfma(vadd(vadd(vadd(vsub(cnN, n), vsub(cnS, n)), vsub(cnE, n)), vsub(cnW, n)),
-                           kt_n, vmul(vadd(vsub(cnT, n), vsub(cnB, n)), kl_n));
-      const V coupi = vfma(vadd(vadd(vadd(vsub(ciN, c), vsub(ciS, c)), vsub(ciE, c)), vsub(ciW, c)),
-                           kt_i, vmul(vadd(vsub(ciT, c), vsub(ciB, c)), kl_i));
+      const V coupn =
+          vfma(vadd(vadd(vadd(vsub(cnN, n), vsub(cnS, n)), vsub(cny_in, n)), vsub(cny_ex, n)), kt_n,
+               vmul(vadd(vsub(cnx_in, n), vsub(cnx_ex, n)), kl_n));
+      const V coupi =
+          vfma(vadd(vadd(vadd(vsub(ciN, c), vsub(ciS, c)), vsub(ciy_in, c)), vsub(ciy_ex, c)), kt_i,
+               vmul(vadd(vsub(cix_in, c), vsub(cix_ex, c)), kl_i));
       // SERCA and leak (subroutine_cuda.c:128-146)
       V up, lk;
       {
-        const R pax = Math<R>::powpos(c.x * R(1.0 / KI_UP), R(HH_UP));
-        const R pay = Math<R>::powpos(c.y * R(1.0 / KI_UP), R(HH_UP));
-        const R pbx = Math<R>::powpos(n.x * R(1.0 / KNSR_UP), R(HH_UP));
-        const R pby = Math<R>::powpos(n.y * R(1.0 / KNSR_UP), R(HH_UP));
+        const R pax = serca_pow<0>(c.x), pay = serca_pow<0>(c.y);
+        const R pbx = serca_pow<1>(n.x), pby = serca_pow<1>(n.y);
         up = v2(k.sviup * Math<R>::div(R(VUP) * (pax - pbx), R(1) + pax + pbx),
                 k.sviup * Math<R>::div(R(VUP) * (pay - pby), R(1) + pay + pby));
         const V n2 = vmul(n, n);
