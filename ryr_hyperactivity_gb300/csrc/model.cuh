@@ -425,21 +425,20 @@ __device__ __forceinline__ void ryr_gating(rh_stream* rng, const StepCoef<R>& k,
 
 // One LCC slot (reesica.h:65-115): a single uniform picks at most one gate
 // flip by first passage over the cumulative rates.
+// Gate b flips from open to closed (st - 2^b) or back (st + 2^b), i.e.
+// st ^ 2^b.  The comparisons keep the reference's order and its running
+// subtraction, so the chosen gate is the same; they are evaluated without
+// branches, which keeps the warp's lanes together.
 template <class R>
 __device__ __forceinline__ int lcc_next(int st, R rig, R ac, R bc, R ad, R bd, R af, R bf,
                                         R afca, R bfca) {
-  R r0 = (st & 1) ? ac : bc;
-  if (rig < r0) return (st & 1) ? st - 1 : st + 1;
-  rig -= r0;
-  R r1 = (st & 2) ? ad : bd;
-  if (rig < r1) return (st & 2) ? st - 2 : st + 2;
-  rig -= r1;
-  R r2 = (st & 4) ? af : bf;
-  if (rig < r2) return (st & 4) ? st - 4 : st + 4;
-  rig -= r2;
-  R r3 = (st & 8) ? afca : bfca;
-  if (rig < r3) return (st & 8) ? st - 8 : st + 8;
-  return st;
+  const R r0 = (st & 1) ? ac : bc;
+  const R r1 = (st & 2) ? ad : bd;
+  const R r2 = (st & 4) ? af : bf;
+  const R r3 = (st & 8) ? afca : bfca;
+  const R g1 = rig - r0, g2 = g1 - r1, g3 = g2 - r2;
+  const int flip = rig < r0 ? 1 : g1 < r1 ? 2 : g2 < r2 ? 4 : g3 < r3 ? 8 : 0;
+  return st ^ flip;
 }
 
 }  // namespace rh
