@@ -90,7 +90,7 @@ __device__ __forceinline__ void fx_warp_sum(uint64_t& lo, uint64_t& hi) {
 // point, the same in every lane.  Cheaper than fx_from + fx_warp_sum: the
 // lanes align their 24-bit mantissas to the warp's largest exponent E
 // (value = m * 2^(e - 150), m scaled by 2^(34 - (E - e)), so 32 of them stay
-// below 2^63) and add them as 64-bit integers in a butterfly; only lanes
+// below 2^63) and add them as 64-bit integers; only lanes
 // more than 2^34 below the warp's largest value lose low bits (an error
 // below 2^-58 of that value).  Integer adds, so the result does not depend
 // on the order of the lanes; `bad` as in fx_from.
@@ -107,8 +107,18 @@ __device__ __forceinline__ void fx_warp_sum_f32(float v, uint64_t& lo, uint64_t&
   const int s = 34 - (int)(E - e);
   int64_t x = s >= 0 ? (int64_t)((uint64_t)m << s) : (s > -32 ? (int64_t)(m >> -s) : 0);
   if (b >> 31) x = -x;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+  // The exact 64-bit sum over the warp as three 32-bit warp reductions:
+  // x = xh 2^32 + xl with |xh| < 2^26 (|x| < 2^58), so the 32 high words
+  // sum within a signed 32-bit integer, and the low words are summed in two
+  // 16-bit halves (each sum below 2^21).
+  {
+    const int32_t xh = (int32_t)(x >> 32);
+    const uint32_t xl = (uint32_t)x;
+    const int32_t sh32 = __reduce_add_sync(0xffffffffu, xh);
+    const uint32_t sa = __reduce_add_sync(0xffffffffu, xl & 0xffffu);
+    const uint32_t sb = __reduce_add_sync(0xffffffffu, xl >> 16);
+    x = (int64_t)((uint64_t)(int64_t)sh32 << 32) + ((int64_t)sb << 16) + (int64_t)sa;
+  }
   // sum * 2^(E - 184) * 2^64 = x * 2^(E - 120), sh in [-120, 47]
   const int sh = (int)E - 120;
   const int64_t sx = x >> 63;  // sign fill
