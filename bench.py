@@ -321,7 +321,8 @@ def main():
                               % (sim.num_groups(), tile)),
                    "autotune_ms_per_update": [
                        {"persistent": t["persistent"], "tile": t["tile_crus"],
-                        "fewer_ctas": t["fewer_ctas"], "groups": t["cell_groups"], "ms": round(m, 4)}
+                        "fewer_ctas": t["fewer_ctas"], "groups": t["cell_groups"],
+                        "bulk_staging": t["bulk_staging"], "ms": round(m, 4)}
                        for t, m in tune]},
         "gpu_launches": kernels,  # counted by the library
         "timed_wall_s": wall,
