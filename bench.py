@@ -12,7 +12,8 @@ every cell.  The state (~1 GB) is far larger than L2, so no flush is needed.
 Printed (rank 0, one JSON line): CRU-updates/s (value), cell-beats/s, the
 step kernel's HBM roofline, the plain FP64 single-cell path (100x20x10) for
 the 10x target, the end-to-end number through the C ABI with host buffers,
-and the CPU oracle baseline.
+and the CPU baseline (the reference's routines built for the host, or the
+oracle port where that build is absent).
 """
 from __future__ import annotations
 
