@@ -147,7 +147,7 @@ typedef struct {
                                  output period) */
   int32_t cell_groups;        /* cells split into this many groups of about equal
                                  CRU count that advance on concurrent streams
-                                 (0 = 16; capped at the number of cells) */
+                                 (0 = 8; capped at the number of cells) */
   int32_t record_cadist;      /* 1 = keep cadist records (the reference's
                                  outputcadist build, :1001-1013): every 5 ms in the
                                  first 500 ms of each pacing period, t, V and 6
@@ -296,6 +296,18 @@ int rh_restore(rh_sim* sim, const char* path);
 int rh_state_bytes(const rh_sim* sim, size_t* bytes);
 int rh_export_state(rh_sim* sim, void* host, size_t bytes);
 int rh_import_state(rh_sim* sim, const void* host, size_t bytes);
+
+/* rh_import_state(host_in) + rh_run_steps(nsteps) + rh_export_state(host_out)
+ * in one call, with the same result.  Either buffer may be NULL (no import,
+ * no export), both may be the same buffer, and `bytes` is rh_state_bytes().
+ * On the two-launch path with pinned (or registered) buffers the copies are
+ * split by cell group: each group's import opens its branch of the first
+ * window and its export closes its branch of the last window, so one group's
+ * copies overlap the other groups' steps.  Otherwise (persistent launch,
+ * pageable buffers) the copies run before and after the steps.  The kernel
+ * timing (rh_kernel_timing) of such a call includes its copies. */
+int rh_run_steps_host(rh_sim* sim, int64_t nsteps, const void* host_in, void* host_out,
+                      size_t bytes);
 
 /* CRU-tile autotuner within the simulator's launch mode.  The step kernel is
  * compiled for tiles of 64, 128 and 256 CRUs per CTA (each with its own

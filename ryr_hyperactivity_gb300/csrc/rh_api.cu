@@ -18,6 +18,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/rh.h"
@@ -76,8 +77,9 @@ struct rh_sim {
   // host staging of rh_drain_wholecell_all: record counters and the record ring
   std::vector<long long> h_counts;
   std::vector<double> h_ring;
-  // graphs keyed by (window length, output-step bitmask)
-  std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
+  // graphs keyed by (window length, output-step bitmask, host buffers of a
+  // state import at the head / export at the tail of each group's branch)
+  std::map<std::tuple<int, std::vector<bool>, const void*, void*>, cudaGraphExec_t> graphs;
   // persistent window launches (run option persistent): per-cell arrival and
   // readiness words with the update queue, the wait-timeout flag, and whether
   // a window launch can be captured in a graph on this device (else it is
@@ -276,22 +278,75 @@ cudaError_t launch_group(rh_sim* s, int g, bool out, bool lattice_only, cudaStre
   return launch_cells<double>(a, c0, c1 - c0, out, t.tile, st);
 }
 
+// The state of cells [c0, c1) between the device and a host image in the
+// layout rh_export_state writes (the arena, then one CellDyn per cell): from
+// `hin` to the device, or from the device to `hout`, on stream `st`.  Cells
+// are consecutive in every plane of the arena, so a group's slice is the same
+// CRU range of each plane: the 10 per-CRU real planes and the 40 sub-voxel
+// pair planes are two strided copies (their planes are equally spaced), the
+// packed integers three more, and the group's CellDyn records one.
+cudaError_t copy_group_state(rh_sim* s, int c0, int c1, const char* hin, char* hout,
+                             cudaStream_t st) {
+  const size_t rs = real_size(s), S = (size_t)s->stride;
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const size_t o0 = (size_t)s->hcells[c0].off;
+  const size_t o1 = c1 < s->ncells ? (size_t)s->hcells[c1].off : S;
+  const size_t sc_pitch = al(S * rs), pair_pitch = 2 * rs * S;
+  const size_t sv_base = 10 * sc_pitch;
+  const size_t ryr_base = sv_base + 10 * al(8 * S * rs);
+  const size_t lcc_base = ryr_base + al(4 * S), win_base = lcc_base + al(8 * S);
+  char* dev = reinterpret_cast<char*>(s->arena);
+  const cudaMemcpyKind kind = hin ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  auto planes = [&](size_t base, size_t pitch, size_t esz, size_t rows) {
+    const size_t off = base + esz * o0, w = esz * (o1 - o0);
+    if (hin) return cudaMemcpy2DAsync(dev + off, pitch, hin + off, pitch, w, rows, kind, st);
+    return cudaMemcpy2DAsync(hout + off, pitch, dev + off, pitch, w, rows, kind, st);
+  };
+  cudaError_t e;
+  if ((e = planes(0, sc_pitch, rs, 10)) != cudaSuccess) return e;
+  if ((e = planes(sv_base, pair_pitch, 2 * rs, 40)) != cudaSuccess) return e;
+  if ((e = planes(ryr_base, 4 * S, 4, 1)) != cudaSuccess) return e;
+  if ((e = planes(lcc_base, 8 * S, 8, 1)) != cudaSuccess) return e;
+  if ((e = planes(win_base, 4 * S, 4, 1)) != cudaSuccess) return e;
+  const size_t doff = s->arena_bytes + sizeof(CellDyn) * (size_t)c0;
+  const size_t dbytes = sizeof(CellDyn) * (size_t)(c1 - c0);
+  char* ddev = reinterpret_cast<char*>(s->d_dyn) + sizeof(CellDyn) * (size_t)c0;
+  return hin ? cudaMemcpyAsync(ddev, hin + doff, dbytes, kind, st)
+             : cudaMemcpyAsync(hout + doff, ddev, dbytes, kind, st);
+}
+
+// Host state image around a run of steps (rh_run_steps_host): imported at
+// the head of the first window, exported at the tail of the last.
+struct HostIO {
+  const char* in = nullptr;
+  char* out = nullptr;
+};
+
 // `n` steps of every group: group g's launches go to its own stream, forked
 // from and joined back to the simulator's stream (inside a capture this
-// makes one graph branch per group).
-cudaError_t launch_steps(rh_sim* s, int n, const bool* outs, bool lattice_only) {
+// makes one graph branch per group).  With `io`, group g's branch begins
+// with the import of its cells' state and ends with their export, so that
+// the copies of one group overlap the other groups' steps.
+cudaError_t launch_steps(rh_sim* s, int n, const bool* outs, bool lattice_only,
+                         const HostIO* io = nullptr) {
+  const char* hin = io ? io->in : nullptr;
+  char* hout = io ? io->out : nullptr;
   if (s->ngroups == 1) {
-    for (int i = 0; i < n; ++i) {
-      cudaError_t e = launch_group(s, 0, outs[i], lattice_only, s->stream);
-      if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    if (hin) e = copy_group_state(s, 0, s->ncells, hin, nullptr, s->stream);
+    for (int i = 0; i < n && e == cudaSuccess; ++i)
+      e = launch_group(s, 0, outs[i], lattice_only, s->stream);
+    if (hout && e == cudaSuccess) e = copy_group_state(s, 0, s->ncells, nullptr, hout, s->stream);
+    return e;
   }
   cudaError_t e = cudaEventRecord(s->gevents[0], s->stream);
   for (int g = 0; g < s->ngroups && e == cudaSuccess; ++g) {
+    const int c0 = s->group_cell[g], c1 = s->group_cell[g + 1];
     e = cudaStreamWaitEvent(s->gstreams[g], s->gevents[0], 0);
+    if (hin && e == cudaSuccess) e = copy_group_state(s, c0, c1, hin, nullptr, s->gstreams[g]);
     for (int i = 0; i < n && e == cudaSuccess; ++i)
       e = launch_group(s, g, outs[i], lattice_only, s->gstreams[g]);
+    if (hout && e == cudaSuccess) e = copy_group_state(s, c0, c1, nullptr, hout, s->gstreams[g]);
     if (e == cudaSuccess) e = cudaEventRecord(s->gevents[1 + g], s->gstreams[g]);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->gevents[1 + g], 0);
   }
@@ -437,14 +492,18 @@ int check_cell(rh_sim* s, int32_t cell) {
 
 // Runs `n` steps in one window: replays (or captures) the graph for this
 // window's pattern of output steps.
-int run_window(rh_sim* s, int n, const std::vector<bool>& outs) {
+int run_window(rh_sim* s, int n, const std::vector<bool>& outs, const HostIO* io = nullptr) {
   const bool persist = use_persist(s);
+  if (persist) io = nullptr;  // the persistent path imports and exports around the window
   if (persist && !s->persist_graph) {  // this device could not capture it: launch directly
     CK(launch_persist(s, n, false));
     return RH_OK;
   }
   // a persistent window reads its output steps on the device: one graph per length
-  auto key = persist ? std::make_pair(-n, std::vector<bool>()) : std::make_pair(n, outs);
+  const void* kin = io ? io->in : nullptr;
+  void* kout = io ? io->out : nullptr;
+  auto key = persist ? std::make_tuple(-n, std::vector<bool>(), kin, kout)
+                     : std::make_tuple(n, outs, kin, kout);
   auto it = s->graphs.find(key);
   cudaGraphExec_t exec = nullptr;
   if (it == s->graphs.end()) {
@@ -452,7 +511,7 @@ int run_window(rh_sim* s, int n, const std::vector<bool>& outs) {
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     std::unique_ptr<bool[]> o(new bool[n]);
     for (int i = 0; i < n; ++i) o[i] = outs[i];
-    cudaError_t le = persist ? launch_persist(s, n, false) : launch_steps(s, n, o.get(), false);
+    cudaError_t le = persist ? launch_persist(s, n, false) : launch_steps(s, n, o.get(), false, io);
     cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
     cudaError_t ie = cudaErrorUnknown;
     if (le == cudaSuccess && ce == cudaSuccess) {
@@ -802,17 +861,80 @@ int rh_destroy(rh_sim* s) {
   return RH_OK;
 }
 
-int rh_run_steps(rh_sim* s, int64_t nsteps) {
+namespace {
+
+// Whether `p` is host memory the GPU can copy from asynchronously (pinned or
+// registered); NULL counts as such.
+bool host_pinned(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// The strided group copies take the 40 sub-voxel pair planes as equally
+// spaced, which holds when a sub-voxel field fills whole 256-byte blocks.
+bool group_copies_ok(const rh_sim* s) {
+  return ((8 * (size_t)s->stride * real_size(s)) % 256) == 0;
+}
+
+// Checks a host state image and points the host mirrors (time, activity,
+// drained records) at the state it holds.
+int import_mirrors(rh_sim* s, const char* h) {
+  const CellDyn* dyn = reinterpret_cast<const CellDyn*>(h + s->arena_bytes);
+  for (int c = 0; c < s->ncells; ++c)
+    if (dyn[c].arrive != 0) return fail(s, RH_ERR_ARG, "import block is not an exported state");
+  for (int c = 0; c < s->ncells; ++c) {
+    s->t_host[c] = dyn[c].m.t;
+    s->active_host[c] = !dyn[c].done;
+    s->drained_wc[c] = std::min(s->drained_wc[c], dyn[c].out_count);
+    s->drained_ls[c] = std::min(s->drained_ls[c], dyn[c].out_count);
+    s->drained_st[c] = std::min(s->drained_st[c], dyn[c].stats_count);
+    s->drained_cd[c] = std::min(s->drained_cd[c], dyn[c].cd_count);
+  }
+  return RH_OK;
+}
+
+cudaError_t copy_state_in(rh_sim* s, const char* h) {
+  cudaError_t e = cudaMemcpyAsync(s->arena, h, s->arena_bytes, cudaMemcpyHostToDevice, s->stream);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(s->d_dyn, h + s->arena_bytes, sizeof(CellDyn) * s->ncells,
+                         cudaMemcpyHostToDevice, s->stream);
+}
+
+cudaError_t copy_state_out(rh_sim* s, char* h) {
+  cudaError_t e = cudaMemcpyAsync(h, s->arena, s->arena_bytes, cudaMemcpyDeviceToHost, s->stream);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(h + s->arena_bytes, s->d_dyn, sizeof(CellDyn) * s->ncells,
+                         cudaMemcpyDeviceToHost, s->stream);
+}
+
+// rh_run_steps, optionally with the state imported from `hin` first and
+// exported to `hout` after (rh_run_steps_host).  On the two-launch path with
+// pinned buffers the copies ride in the first and the last window, per cell
+// group; otherwise they run before and after the steps.
+int run_steps_impl(rh_sim* s, int64_t nsteps, const char* hin, char* hout) {
   if (!s || nsteps < 0) return RH_ERR_ARG;
   if (!s->stream) return fail(s, RH_ERR_STATE, "simulator not initialised");
+  CK(cudaSetDevice(s->device));
+  const bool pipe = (hin || hout) && !use_persist(s) && group_copies_ok(s) && host_pinned(hin) &&
+                    host_pinned(hout);
+  if (hin) {
+    int r = import_mirrors(s, hin);
+    if (r) return r;
+  }
   for (int c = 0; c < s->ncells; ++c)
     if (s->active_host[c] && s->hcells[c].protocol == RH_PROTO_AP_CLAMP && !s->hcells[c].apv)
       return fail(s, RH_ERR_STATE, "cell %d: AP-clamp waveform not set (rh_set_ap_clamp)", c);
-  CK(cudaSetDevice(s->device));
   if (s->opts.keep_diagnostics) {
     int r = ensure_diag(s);
     if (r) return r;
   }
+  if (hin && !pipe) CK(copy_state_in(s, hin));
+  bool in_pending = hin && pipe, out_pending = hout != nullptr;
   const double dt = s->opts.dt_ms;
   const int W = s->opts.window_steps;
   int64_t done = 0;
@@ -840,26 +962,49 @@ int rh_run_steps(rh_sim* s, int64_t nsteps) {
       }
     }
     if (k == 0) break;
+    bool any_left = false;
+    for (int c = 0; c < s->ncells; ++c) any_left = any_left || s->active_host[c];
+    HostIO io;
+    if (in_pending) io.in = hin;
+    if (pipe && hout && (done + k >= nsteps || !any_left)) io.out = hout;
+    const HostIO* iop = (io.in || io.out) ? &io : nullptr;
     int r;
     const bool persist = use_persist(s);
     if (k == W) {
-      r = run_window(s, k, outs);
+      r = run_window(s, k, outs, iop);
     } else {
       r = RH_OK;
       std::unique_ptr<bool[]> o(new bool[k]);
       for (int i = 0; i < k; ++i) o[i] = outs[i];
-      cudaError_t e = persist ? launch_persist(s, k, false) : launch_steps(s, k, o.get(), false);
+      cudaError_t e = persist ? launch_persist(s, k, false) : launch_steps(s, k, o.get(), false, iop);
       if (e != cudaSuccess) return fail(s, RH_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
     }
     if (r) return r;
+    if (io.in) in_pending = false;
+    if (io.out) out_pending = false;
     s->kernels += persist ? 1 : 2LL * s->ngroups * k;
     nlaunch += k;
     done += k;
   }
+  if (in_pending) CK(copy_state_in(s, hin));  // no step ran
+  if (out_pending) CK(copy_state_out(s, hout));
   timing_end(s, nlaunch);
   CK(cudaStreamSynchronize(s->stream));
   CK(cudaGetLastError());
   return check_wait_error(s);
+}
+
+}  // namespace
+
+int rh_run_steps(rh_sim* s, int64_t nsteps) { return run_steps_impl(s, nsteps, nullptr, nullptr); }
+
+int rh_run_steps_host(rh_sim* s, int64_t nsteps, const void* host_in, void* host_out,
+                      size_t bytes) {
+  if (!s || nsteps < 0) return RH_ERR_ARG;
+  if ((host_in || host_out) && bytes != s->arena_bytes + sizeof(CellDyn) * (size_t)s->ncells)
+    return fail(s, RH_ERR_ARG, "state buffers must hold rh_state_bytes() bytes");
+  return run_steps_impl(s, nsteps, reinterpret_cast<const char*>(host_in),
+                        reinterpret_cast<char*>(host_out));
 }
 
 int rh_run_to_end(rh_sim* s) {
@@ -1406,10 +1551,7 @@ int rh_export_state(rh_sim* s, void* host, size_t bytes) {
   if (!s || !host || bytes != s->arena_bytes + sizeof(CellDyn) * (size_t)s->ncells)
     return fail(s, RH_ERR_ARG, "export buffer must hold rh_state_bytes() bytes");
   CK(cudaSetDevice(s->device));
-  char* h = reinterpret_cast<char*>(host);
-  CK(cudaMemcpyAsync(h, s->arena, s->arena_bytes, cudaMemcpyDeviceToHost, s->stream));
-  CK(cudaMemcpyAsync(h + s->arena_bytes, s->d_dyn, sizeof(CellDyn) * s->ncells,
-                     cudaMemcpyDeviceToHost, s->stream));
+  CK(copy_state_out(s, reinterpret_cast<char*>(host)));
   CK(cudaStreamSynchronize(s->stream));
   return RH_OK;
 }
@@ -1419,20 +1561,9 @@ int rh_import_state(rh_sim* s, const void* host, size_t bytes) {
     return fail(s, RH_ERR_ARG, "import buffer must hold rh_state_bytes() bytes");
   CK(cudaSetDevice(s->device));
   const char* h = reinterpret_cast<const char*>(host);
-  const CellDyn* dyn = reinterpret_cast<const CellDyn*>(h + s->arena_bytes);
-  for (int c = 0; c < s->ncells; ++c)
-    if (dyn[c].arrive != 0) return fail(s, RH_ERR_ARG, "import block is not an exported state");
-  CK(cudaMemcpyAsync(s->arena, h, s->arena_bytes, cudaMemcpyHostToDevice, s->stream));
-  CK(cudaMemcpyAsync(s->d_dyn, dyn, sizeof(CellDyn) * s->ncells, cudaMemcpyHostToDevice,
-                     s->stream));
-  for (int c = 0; c < s->ncells; ++c) {
-    s->t_host[c] = dyn[c].m.t;
-    s->active_host[c] = !dyn[c].done;
-    s->drained_wc[c] = std::min(s->drained_wc[c], dyn[c].out_count);
-    s->drained_ls[c] = std::min(s->drained_ls[c], dyn[c].out_count);
-    s->drained_st[c] = std::min(s->drained_st[c], dyn[c].stats_count);
-    s->drained_cd[c] = std::min(s->drained_cd[c], dyn[c].cd_count);
-  }
+  int r = import_mirrors(s, h);
+  if (r) return r;
+  CK(copy_state_in(s, h));
   CK(cudaStreamSynchronize(s->stream));
   return RH_OK;
 }

@@ -18,7 +18,7 @@ constexpr int kDefaultTile = 128;
 // chain of dependent FP64 work that leaves most SMs to the other groups; with
 // 16 groups (512 cells, mixed precision) the step took 0.524 ms against
 // 0.542 ms with 4 groups.
-constexpr int kDefaultGroups = 16;
+constexpr int kDefaultGroups = 8;
 
 // Resident CTAs per SM each instantiation's register allocation is bounded
 // for.  FP32: about 640 threads per SM at <= ~100 registers (measured best:

@@ -22,6 +22,7 @@ EXPORTS = [
     "rh_format_linescan", "rh_state_bytes", "rh_export_state", "rh_import_state",
     "rh_analyze_trace", "rh_autotune", "rh_tile_size", "rh_kernel_launches", "rh_set_wait_limit",
     "rh_window_ctas", "rh_get_launch_shape", "rh_set_launch_shape", "rh_autotune_shapes",
+    "rh_run_steps_host",
 ]
 
 _lib = None
@@ -47,6 +48,7 @@ def load() -> C.CDLL:
     L.rh_create.argtypes = [C.POINTER(CellParams), C.c_int32, C.POINTER(RunOpts), C.POINTER(vp)]
     L.rh_destroy.argtypes = [vp]
     L.rh_run_steps.argtypes = [vp, C.c_int64]
+    L.rh_run_steps_host.argtypes = [vp, C.c_int64, vp, vp, C.c_size_t]
     L.rh_run_to_end.argtypes = [vp]
     L.rh_lattice_step.argtypes = [vp]
     L.rh_num_cells.argtypes = [vp, C.POINTER(C.c_int32)]

@@ -174,6 +174,13 @@ class Simulator:
     def import_state(self, ptr: int, nbytes: int) -> None:
         self._ck(self.L.rh_import_state(self.h, C.c_void_p(ptr), nbytes))
 
+    def run_steps_host(self, n: int, in_ptr: int | None, out_ptr: int | None, nbytes: int) -> None:
+        """import_state(in_ptr) + run_steps(n) + export_state(out_ptr) in one
+        call (rh_run_steps_host); with pinned buffers the copies of each cell
+        group overlap the other groups' steps.  Either address may be None."""
+        self._ck(self.L.rh_run_steps_host(self.h, int(n), C.c_void_p(in_ptr or 0),
+                                          C.c_void_p(out_ptr or 0), nbytes))
+
     def autotune(self, steps: int = 50) -> tuple[int, list[float]]:
         """Picks the fastest tile length for this workload; returns it and the
         measured ms per step of each candidate (64, 128, 256 CRUs)."""
