@@ -333,10 +333,13 @@ typedef struct {
                            fewer than the step kernel holds, with more registers
                            per thread (cells without build options only) */
   int32_t cell_groups;  /* two-launch path: cell groups on concurrent streams */
-  int32_t bulk_staging; /* two-launch path, FP32 lattice: 1 = a tile's own state
-                           and its stencil halo rows arrive by bulk asynchronous
-                           copies issued by one warp (completion on mbarriers),
-                           0 = every thread copies its share with cp.async */
+  int32_t bulk_staging; /* two-launch path, FP32 lattice: 0 = every thread
+                           copies its share with cp.async; 1 = a tile's own
+                           state and its stencil halo rows arrive by bulk
+                           asynchronous copies issued by one warp (completion
+                           on mbarriers); 2 = the tile's ci/cnsr pair planes and
+                           its eight real planes arrive as 2-D tensor tiles
+                           (cp.async.bulk.tensor, one thread), the rest as in 0 */
 } rh_launch_shape;
 
 int rh_get_launch_shape(const rh_sim* sim, rh_launch_shape* shape);

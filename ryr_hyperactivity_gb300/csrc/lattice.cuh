@@ -19,6 +19,7 @@
 // terms are dropped and the z-ghost of cs reads the CRU's own value.
 #pragma once
 
+#include <cuda.h>
 #include <stdint.h>
 
 #include "../../include/rh.h"
@@ -127,6 +128,16 @@ template <>
 __device__ __forceinline__ const StepCoef<float>* coef_ptr<float>(const CellDyn* d) {
   return &d->cf;
 }
+
+// Tensor maps of the tensor-copy staging (FP32 only): the pair planes of ci
+// and cnsr of each ping-pong parity as 2-D tensors of 8-byte pairs (x: arena
+// index, y: pair plane; box B x 4), and the eight per-CRU real planes
+// cp .. casarhj as a 2-D tensor of floats (box B x 8).  Built on the host per
+// tile length, passed to the lattice launch as a grid constant.
+struct StageMaps {
+  CUtensorMap plane[4];  // ci[0], ci[1], cnsr[0], cnsr[1]
+  CUtensorMap sc;
+};
 
 template <class R>
 struct StepArgs {

@@ -5,6 +5,7 @@
 // of steps as captured CUDA graphs,
 // mirrors each cell's time on the host to know which steps are output steps,
 // and moves state and output records between host and device.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
@@ -87,7 +88,10 @@ struct rh_sim {
   bool persist_ok = false;
   bool persist_graph = true;
   bool fewer_ctas = false;  // persistent launch at one resident CTA per SM fewer
-  bool bulk = false;        // two-launch path: FP32 staging by bulk asynchronous copies
+  int staging = 0;          // two-launch path, FP32: 0 per-thread, 1 bulk, 2 tensor copies
+  // tensor maps of the tensor-copy staging, one set per tile length (FP32)
+  StageMaps maps[kNumTileSizes]{};
+  bool maps_ok = false;
   CellSync* d_sync = nullptr;
   unsigned int* d_err = nullptr;
   unsigned int* h_err = nullptr;  // pinned
@@ -226,6 +230,59 @@ void carve(Lattice<R>& L, char*& p, int64_t S) {
   L.win = reinterpret_cast<uint32_t*>(takeu(S * 4));
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once per process.
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn tensor_map_encoder() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// The tensor maps of the FP32 lattice's tensor-copy staging for tiles of
+// `tile` CRUs.  The encoder checks the base addresses (256-byte aligned
+// planes), the pitches (multiples of 256 bytes) and the boxes (at most 256
+// elements a side, B x 8 or B x 4 bytes inner extent); the kernels' x
+// coordinate, a tile's first arena index, is a multiple of 32.
+bool build_stage_maps(const Lattice<float>& L, int64_t stride, int tile, StageMaps& m) {
+  EncodeTiledFn enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t S = (cuuint64_t)stride;
+  const cuuint32_t one[2] = {1, 1};
+  // pair planes: 8-byte pairs, 4 planes of S pairs, 8 S bytes apart
+  const cuuint64_t pdim[2] = {S, 4}, pstride[1] = {8 * S};
+  const cuuint32_t pbox[2] = {(cuuint32_t)tile, 4};
+  float* planes[4] = {L.ci[0], L.ci[1], L.cnsr[0], L.cnsr[1]};
+  for (int i = 0; i < 4; ++i)
+    if (enc(&m.plane[i], CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, planes[i], pdim, pstride, pbox, one,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  // the eight real planes cp .. casarhj, equally spaced
+  const float* sc[8] = {L.cp, L.cjsr, L.cjsrb, L.ancx, L.casar, L.casarh, L.casarj, L.casarhj};
+  const ptrdiff_t pitch = reinterpret_cast<const char*>(sc[1]) - reinterpret_cast<const char*>(sc[0]);
+  for (int i = 1; i < 8; ++i)
+    if (reinterpret_cast<const char*>(sc[i]) - reinterpret_cast<const char*>(sc[i - 1]) != pitch)
+      return false;
+  const cuuint64_t sdim[2] = {S, 8}, sstride[1] = {(cuuint64_t)pitch};
+  const cuuint32_t sbox[2] = {(cuuint32_t)tile, 8};
+  return enc(&m.sc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, L.cp, sdim, sstride, sbox, one,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 size_t lattice_bytes(size_t rs, int64_t S) {
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
   // 10 per-CRU real fields (cs twice), 10 sub-voxel fields (8 values per CRU,
@@ -266,14 +323,16 @@ cudaError_t launch_group(rh_sim* s, int g, bool out, bool lattice_only, cudaStre
     StepArgs<float> a = make_args(s, s->Lf, lattice_only);
     a.tiles += tb;
     a.tile_base = tb;
-    if ((e = launch_step<float>(a, te - tb, out, s->group_opt[g], t.tile, s->bulk, st)) != cudaSuccess)
+    if ((e = launch_step<float>(a, te - tb, out, s->group_opt[g], t.tile, s->staging,
+                                &s->maps[s->ts], st)) != cudaSuccess)
       return e;
     return launch_cells<float>(a, c0, c1 - c0, out, t.tile, st);
   }
   StepArgs<double> a = make_args(s, s->Ld, lattice_only);
   a.tiles += tb;
   a.tile_base = tb;
-  if ((e = launch_step<double>(a, te - tb, out, s->group_opt[g], t.tile, false, st)) != cudaSuccess)
+  if ((e = launch_step<double>(a, te - tb, out, s->group_opt[g], t.tile, 0, nullptr, st)) !=
+      cudaSuccess)
     return e;
   return launch_cells<double>(a, c0, c1 - c0, out, t.tile, st);
 }
@@ -757,6 +816,11 @@ static int create_impl(rh_sim* s, const rh_cell_params* cells, int32_t ncells,
   char* p = reinterpret_cast<char*>(s->arena);
   if (is_mixed(s)) carve(s->Lf, p, s->stride);
   else carve(s->Ld, p, s->stride);
+  if (is_mixed(s)) {
+    s->maps_ok = true;
+    for (int k = 0; k < kNumTileSizes; ++k)
+      s->maps_ok = s->maps_ok && build_stage_maps(s->Lf, s->stride, kTileSizes[k], s->maps[k]);
+  }
   CK(cudaMalloc(&s->d_dyn, sizeof(CellDyn) * ncells));
   for (int k = 0; k < kNumTileSizes; ++k) {
     rh_sim::TileSet& t = s->sets[k];
@@ -1657,7 +1721,7 @@ int rh_get_launch_shape(const rh_sim* s, rh_launch_shape* shape) {
   shape->tile_crus = s->sets[s->ts].tile;
   shape->fewer_ctas = (shape->persistent && s->fewer_ctas) ? 1 : 0;
   shape->cell_groups = s->ngroups;
-  shape->bulk_staging = (!shape->persistent && s->bulk) ? 1 : 0;
+  shape->bulk_staging = shape->persistent ? 0 : s->staging;
   return RH_OK;
 }
 
@@ -1677,15 +1741,19 @@ int rh_set_launch_shape(rh_sim* s, const rh_launch_shape* shape) {
     if (shape->bulk_staging)
       return fail(s, RH_ERR_NOTBUILT, "bulk staging is compiled for the two-launch path");
   }
+  if (shape->bulk_staging < 0 || shape->bulk_staging > 2)
+    return fail(s, RH_ERR_ARG, "bulk_staging is 0, 1 or 2");
   if (shape->bulk_staging && !is_mixed(s))
     return fail(s, RH_ERR_NOTBUILT, "bulk staging is compiled for the FP32 lattice");
+  if (shape->bulk_staging == 2 && !s->maps_ok)
+    return fail(s, RH_ERR_NOTBUILT, "tensor copies need the driver's tensor-map encoder");
   CK(cudaSetDevice(s->device));
   CK(cudaStreamSynchronize(s->stream));
   s->ts = k;
   s->hcells = s->sets[k].hcells;
   s->opts.persistent = shape->persistent ? 1 : 0;
   s->fewer_ctas = shape->persistent && shape->fewer_ctas;
-  s->bulk = !shape->persistent && shape->bulk_staging;
+  s->staging = shape->persistent ? 0 : shape->bulk_staging;
   if (!shape->persistent && shape->cell_groups > 0 && shape->cell_groups != s->ngroups) {
     int r = set_groups(s, shape->cell_groups);
     if (r) return r;
@@ -1746,7 +1814,7 @@ int rh_autotune_shapes(rh_sim* s, int32_t steps, rh_launch_shape* best,
     for (int tile : {64, 128})
       for (int fewer = 0; fewer < (any_options(s) ? 1 : 2); ++fewer)
         cand.push_back(rh_launch_shape{1, tile, fewer, 0, 0});
-  for (int bulk = 0; bulk < (is_mixed(s) ? 2 : 1); ++bulk)
+  for (int bulk = 0; bulk < (is_mixed(s) ? (s->maps_ok ? 3 : 2) : 1); ++bulk)
     for (int tile : {64, 128, 256})
       for (int g : {8, 12, 16, 24})
         if (g <= s->ncells || g == 8)

@@ -30,19 +30,21 @@ __global__ void __launch_bounds__(32, 16) cell_kernel(StepArgs<R> a, int cell0, 
   cell_update<R, OUT, false>(a, cell0 + blockIdx.x, nw, scratch);
 }
 
-template <class R, bool OUT, int B, bool OPT, bool BULK>
-__global__ void __launch_bounds__(B, min_blocks_for<R, B>()) step_kernel(StepArgs<R> a) {
+template <class R, bool OUT, int B, bool OPT, int STG>
+__global__ void __launch_bounds__(B, min_blocks_for<R, B>())
+    step_kernel(StepArgs<R> a, const __grid_constant__ StageMaps maps) {
   __shared__ TileHeader sh;
   __shared__ StepCoef<R> sk;
-  __shared__ __align__(8) uint64_t bars[2];  // bulk staging: channel data, halo rows
-  extern __shared__ __align__(16) unsigned char dsm[];
+  // bulk staging: channel data, halo rows; tensor staging: real planes, pair planes
+  __shared__ __align__(8) uint64_t bars[2];
+  extern __shared__ __align__(128) unsigned char dsm[];  // tensor copies land 128-byte aligned
   allow_dependent_launch();  // the cell update may start its first part
-  if (BULK && threadIdx.x == 0) {  // ordered before their use by the header barrier
+  if (STG != 0 && threadIdx.x == 0) {  // ordered before the other threads' waits by the header barrier
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  tile_update<R, OUT, B, OPT, BULK>(a, blockIdx.x, sh, sk, dsm, bars, 0u);
+  tile_update<R, OUT, B, OPT, STG>(a, blockIdx.x, sh, sk, dsm, bars, 0u, &maps);
 }
 
 // ------------------------------------------------------------- other kernels
@@ -122,64 +124,78 @@ __global__ void coef_prep_kernel(const CellConst* cells, CellDyn* dyn, int ncell
 
 // Instantiations whose tile needs more than the default 48 KB of dynamic
 // shared memory opt in once per device (before any launch or capture).
-template <class R, int B, bool BULK>
+template <class R, int B, int STG>
 cudaError_t opt_in_smem() {
-  constexpr size_t smem = BULK ? TileSmem<R, B>::kBytesBulk : TileSmem<R, B>::kBytes;
+  constexpr size_t smem = STG == 1 ? TileSmem<R, B>::kBytesBulk : TileSmem<R, B>::kBytes;
   if (smem <= 48 * 1024) return cudaSuccess;
   const cudaFuncAttribute attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(step_kernel<R, true, B, false, BULK>, attr, (int)smem))) return e;
-  if ((e = cudaFuncSetAttribute(step_kernel<R, false, B, false, BULK>, attr, (int)smem))) return e;
-  if ((e = cudaFuncSetAttribute(step_kernel<R, true, B, true, BULK>, attr, (int)smem))) return e;
-  return cudaFuncSetAttribute(step_kernel<R, false, B, true, BULK>, attr, (int)smem);
+  if ((e = cudaFuncSetAttribute(step_kernel<R, true, B, false, STG>, attr, (int)smem))) return e;
+  if ((e = cudaFuncSetAttribute(step_kernel<R, false, B, false, STG>, attr, (int)smem))) return e;
+  if ((e = cudaFuncSetAttribute(step_kernel<R, true, B, true, STG>, attr, (int)smem))) return e;
+  return cudaFuncSetAttribute(step_kernel<R, false, B, true, STG>, attr, (int)smem);
+}
+
+template <int B>
+cudaError_t opt_in_smem_f32() {
+  cudaError_t e;
+  if ((e = opt_in_smem<float, B, 0>()) != cudaSuccess) return e;
+  if ((e = opt_in_smem<float, B, 1>()) != cudaSuccess) return e;
+  return opt_in_smem<float, B, 2>();
 }
 
 cudaError_t prepare_step_kernels() {
   cudaError_t e;
-  if ((e = opt_in_smem<float, 64, false>()) != cudaSuccess) return e;
-  if ((e = opt_in_smem<float, 128, false>()) != cudaSuccess) return e;
-  if ((e = opt_in_smem<float, 256, false>()) != cudaSuccess) return e;
-  if ((e = opt_in_smem<float, 64, true>()) != cudaSuccess) return e;
-  if ((e = opt_in_smem<float, 128, true>()) != cudaSuccess) return e;
-  if ((e = opt_in_smem<float, 256, true>()) != cudaSuccess) return e;
-  if ((e = opt_in_smem<double, 64, false>()) != cudaSuccess) return e;
-  if ((e = opt_in_smem<double, 128, false>()) != cudaSuccess) return e;
-  return opt_in_smem<double, 256, false>();
+  if ((e = opt_in_smem_f32<64>()) != cudaSuccess) return e;
+  if ((e = opt_in_smem_f32<128>()) != cudaSuccess) return e;
+  if ((e = opt_in_smem_f32<256>()) != cudaSuccess) return e;
+  if ((e = opt_in_smem<double, 64, 0>()) != cudaSuccess) return e;
+  if ((e = opt_in_smem<double, 128, 0>()) != cudaSuccess) return e;
+  return opt_in_smem<double, 256, 0>();
 }
 
-template <class R, int B, bool BULK>
-void launch_bb(const StepArgs<R>& a, int ntiles, bool out, bool opt, cudaStream_t st) {
-  constexpr size_t smem = BULK ? TileSmem<R, B>::kBytesBulk : TileSmem<R, B>::kBytes;
+template <class R, int B, int STG>
+void launch_bb(const StepArgs<R>& a, const StageMaps& maps, int ntiles, bool out, bool opt,
+               cudaStream_t st) {
+  constexpr size_t smem = STG == 1 ? TileSmem<R, B>::kBytesBulk : TileSmem<R, B>::kBytes;
   if (opt) {
-    if (out) step_kernel<R, true, B, true, BULK><<<ntiles, B, smem, st>>>(a);
-    else step_kernel<R, false, B, true, BULK><<<ntiles, B, smem, st>>>(a);
+    if (out) step_kernel<R, true, B, true, STG><<<ntiles, B, smem, st>>>(a, maps);
+    else step_kernel<R, false, B, true, STG><<<ntiles, B, smem, st>>>(a, maps);
   } else {
-    if (out) step_kernel<R, true, B, false, BULK><<<ntiles, B, smem, st>>>(a);
-    else step_kernel<R, false, B, false, BULK><<<ntiles, B, smem, st>>>(a);
+    if (out) step_kernel<R, true, B, false, STG><<<ntiles, B, smem, st>>>(a, maps);
+    else step_kernel<R, false, B, false, STG><<<ntiles, B, smem, st>>>(a, maps);
   }
 }
 
-// Bulk staging is compiled for the FP32 lattice only (the FP64 kernels
-// read global memory directly).
+// Bulk and tensor staging are compiled for the FP32 lattice only (the FP64
+// kernels read global memory directly).
 template <class R, int B>
-void launch_b(const StepArgs<R>& a, int ntiles, bool out, bool opt, bool bulk, cudaStream_t st) {
+void launch_b(const StepArgs<R>& a, const StageMaps& maps, int ntiles, bool out, bool opt,
+              int staging, cudaStream_t st) {
   if constexpr (sizeof(R) == 4) {
-    if (bulk) {
-      launch_bb<R, B, true>(a, ntiles, out, opt, st);
+    if (staging == 1) {
+      launch_bb<R, B, 1>(a, maps, ntiles, out, opt, st);
+      return;
+    }
+    if (staging == 2) {
+      launch_bb<R, B, 2>(a, maps, ntiles, out, opt, st);
       return;
     }
   }
-  launch_bb<R, B, false>(a, ntiles, out, opt, st);
+  launch_bb<R, B, 0>(a, maps, ntiles, out, opt, st);
 }
 
 template <class R>
-cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, bool opt, int tile, bool bulk,
-                        cudaStream_t st) {
+cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, bool opt, int tile,
+                        int staging, const StageMaps* maps, cudaStream_t st) {
   if (ntiles <= 0) return cudaSuccess;
+  if (staging == 2 && !maps) return cudaErrorInvalidValue;
+  static const StageMaps kNoMaps{};
+  const StageMaps& m = maps ? *maps : kNoMaps;
   switch (tile) {
-    case 64: launch_b<R, 64>(a, ntiles, out, opt, bulk, st); break;
-    case 128: launch_b<R, 128>(a, ntiles, out, opt, bulk, st); break;
-    case 256: launch_b<R, 256>(a, ntiles, out, opt, bulk, st); break;
+    case 64: launch_b<R, 64>(a, m, ntiles, out, opt, staging, st); break;
+    case 128: launch_b<R, 128>(a, m, ntiles, out, opt, staging, st); break;
+    case 256: launch_b<R, 256>(a, m, ntiles, out, opt, staging, st); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -229,10 +245,10 @@ cudaError_t launch_volt_prep(const CellConst* cells, CellDyn* dyn, int ncells, d
   return cudaGetLastError();
 }
 
-template cudaError_t launch_step<double>(const StepArgs<double>&, int, bool, bool, int, bool,
-                                         cudaStream_t);
-template cudaError_t launch_step<float>(const StepArgs<float>&, int, bool, bool, int, bool,
-                                        cudaStream_t);
+template cudaError_t launch_step<double>(const StepArgs<double>&, int, bool, bool, int, int,
+                                         const StageMaps*, cudaStream_t);
+template cudaError_t launch_step<float>(const StepArgs<float>&, int, bool, bool, int, int,
+                                        const StageMaps*, cudaStream_t);
 template cudaError_t launch_cells<double>(const StepArgs<double>&, int, int, bool, int,
                                           cudaStream_t);
 template cudaError_t launch_cells<float>(const StepArgs<float>&, int, int, bool, int,

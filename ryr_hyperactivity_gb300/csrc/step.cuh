@@ -90,10 +90,11 @@ cudaError_t window_grid(int tile, bool opt, bool fewer_ctas, int* ctas);
 // the kernel variant that handles the per-cell build options of the lattice
 // update (perm, iso, slowncxchange, NCX form); without them a cell runs the
 // plain variant.
-// `bulk` selects the staging by bulk asynchronous copies (FP32 only).
+// `staging` selects the FP32 kernels' staging (0 per-thread copies, 1 bulk
+// asynchronous copies, 2 tensor copies through `maps`, built for `tile`).
 template <class R>
-cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, bool opt, int tile, bool bulk,
-                        cudaStream_t st);
+cudaError_t launch_step(const StepArgs<R>& a, int ntiles, bool out, bool opt, int tile,
+                        int staging, const StageMaps* maps, cudaStream_t st);
 
 // The whole-cell update of cells [cell0, cell0 + ncells) after their lattice
 // launch on the same stream (`tile` is the lattice launch's tile length).

@@ -10,6 +10,7 @@
 // coefficients of the next step.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -284,6 +285,17 @@ __device__ __forceinline__ void bulk_row(void* dst, const void* row, long long f
       : "memory");
 }
 
+// One 2-D tile of a tensor into shared memory (dst 128-byte aligned), its
+// bytes counted on `bar`.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
 struct TileHeader {
   int lx, ly, lz, nxf, nyf, tile_count, line_y, line_z;
   uint32_t seed, cell_id;
@@ -301,19 +313,28 @@ struct TileHeader {
 // Per-cell state is read through L2 (__ldcg): inside the persistent window
 // kernel other CTAs write it during the launch.
 //
-// BULK (FP32 only) stages with bulk asynchronous copies issued by warp 0 into
-// two mbarriers (`bars`, initialised with one arrival each, phase `phase`):
-// the tile's own planes, scalars, integers and the cs of its z neighbours,
-// then the y and z halo rows; otherwise every thread issues cp.async copies
-// of its own share and of its CRU's halo.
-template <class R, bool OUT, int B, bool OPT, bool BULK = false>
+// STG selects the staging of the FP32 kernels (the FP64 kernels stage only
+// their own pair planes, with plain loads):
+//   0: every thread issues cp.async copies of its share of the tile's own
+//      data and of its CRU's halo;
+//   1: warp 0 issues bulk asynchronous copies (the TMA engine's linear mode)
+//      into two mbarriers (`bars`, one arrival each, phase `phase`): the
+//      tile's own planes, scalars, integers and the cs of its z neighbours,
+//      then the y and z halo rows;
+//   2: thread 0 issues 2-D tensor copies (cp.async.bulk.tensor, `maps`) of the
+//      tile's eight per-CRU real planes (bars[0], before the cell header
+//      arrives) and of its ci and cnsr pair planes (bars[1]); the integers,
+//      cs and the halo stay per-thread copies as in 0.
+template <class R, bool OUT, int B, bool OPT, int STG = 0>
 __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHeader& sh,
                                             StepCoef<R>& sk, unsigned char* dsm,
-                                            uint64_t* bars = nullptr, uint32_t phase = 0) {
+                                            uint64_t* bars = nullptr, uint32_t phase = 0,
+                                            const StageMaps* maps = nullptr) {
   constexpr int kBlock = B;
   using TS = TileSmem<R, B>;
   constexpr bool kStage = TS::kStage;
-  static_assert(!BULK || kStage, "bulk staging is the FP32 staging");
+  constexpr bool BULK = STG == 1, TMA = STG == 2;
+  static_assert(STG == 0 || kStage, "bulk and tensor staging are the FP32 staging");
   using V = typename Vec2<R>::T;
   V(*s_ci2)[kBlock] = reinterpret_cast<V(*)[kBlock]>(dsm + TS::kCi);
   V(*s_cn2)[kBlock] = reinterpret_cast<V(*)[kBlock]>(dsm + TS::kCn);
@@ -346,9 +367,14 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
     if (kSS && h2 == 0 && 2 * c2 < cpad) cp_async16(&s_lcc[2 * c2], L.lcc + gt0 + 2 * c2);
     constexpr int kTpq = kBlock / 4;  // threads per 4-byte plane
     const int c4 = tid % kTpq, h4 = tid / kTpq;
+    if (TMA && tid == 0) {  // the eight real planes as one tensor tile
+      mbar_expect_tx(&bars[0], 8u * kBlock * sizeof(R));
+      tma_load_2d(&s_sc[0][0], &maps->sc, (int)gt0, 0, &bars[0]);
+      mbar_arrive(&bars[0]);
+    }
     if (kSS && 4 * c4 < cpad) {
 #pragma unroll
-      for (int f = 0; f < 10; ++f) {  // cp cjsr cjsrb ancx casar casarh casarj casarhj ryr win
+      for (int f = TMA ? 8 : 0; f < 10; ++f) {  // cp cjsr cjsrb ancx casar casarh casarj casarhj ryr win
         if ((f & 3) != h4) continue;
         const void* src = f == 0 ? (const void*)(L.cp + gt0) : f == 1 ? (const void*)(L.cjsr + gt0)
                         : f == 2 ? (const void*)(L.cjsrb + gt0) : f == 3 ? (const void*)(L.ancx + gt0)
@@ -392,6 +418,7 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
   __syncthreads();
   if (sh.done) {
     if (kStage) cp_async_wait_all();  // no copy may still target this CTA's shared memory
+    if (TMA) mbar_wait(&bars[0], phase);
     return false;
   }
 
@@ -485,7 +512,13 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
   if (kStage && !BULK) {
     constexpr int kTpp = kBlock / 2;
     const int c2 = tid % kTpp, h2 = tid / kTpp;
-    if (2 * c2 < cpad) {
+    if (TMA && tid == 0) {  // ci and cnsr of this parity: one tensor tile each
+      mbar_expect_tx(&bars[1], 2u * 4u * kBlock * sizeof(V));
+      tma_load_2d(&s_ci2[0][0], &maps->plane[par], (int)gt0, 0, &bars[1]);
+      tma_load_2d(&s_cn2[0][0], &maps->plane[2 + par], (int)gt0, 0, &bars[1]);
+      mbar_arrive(&bars[1]);
+    }
+    if (!TMA && 2 * c2 < cpad) {
 #pragma unroll
       for (int k = 0; k < 4; ++k) {  // ci and cnsr, 4 pair planes each
         const int pl = 2 * (k & 1) + h2;
@@ -527,6 +560,8 @@ __device__ __forceinline__ bool tile_update(const StepArgs<R>& a, int ti, TileHe
     }
     cp_async_commit();       // group 2: the halo, which only its own thread reads
     cp_async_wait_group<1>();  // group 1 has landed (this thread's part of it)
+    if (TMA && !(mbar_wait(&bars[0], phase) && mbar_wait(&bars[1], phase)))
+      atomicOr(&a.dyn[cell].status, (unsigned int)RH_STATUS_TIMEOUT);
   } else if (!kStage) {
 #pragma unroll
     for (int p = 0; p < 4; ++p) {

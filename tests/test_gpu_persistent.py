@@ -111,9 +111,9 @@ def test_shape_autotuner_restores_state_and_caches_its_choice():
         b.run_steps(150)
         best, tried = a.autotune_shapes(8)
         # 4 persistent shapes; 3 tile lengths at one group count (6 cells cap
-        # it), with either staging
-        assert len(tried) == 10 and all(ms > 0 for _, ms in tried)
-        assert {t["bulk_staging"] for t, _ in tried} == {0, 1}
+        # it), with each of the three stagings
+        assert len(tried) == 13 and all(ms > 0 for _, ms in tried)
+        assert {t["bulk_staging"] for t, _ in tried} == {0, 1, 2}
         assert {t["persistent"] for t, _ in tried} == {0, 1}
         assert a.launch_shape()["tile_crus"] == best["tile_crus"]
         assert a.get_membrane(0).step == 150

@@ -1,6 +1,7 @@
-"""Bulk-copy staging of the FP32 lattice update against per-thread cp.async
-staging: the same arithmetic on the same data, so the two must agree bit for
-bit.  The lattices cover every alignment of the halo rows the bulk copies move
+"""Bulk-copy staging (bulk_staging 1) and tensor-copy staging (2, the tile's
+own pair planes and real planes as 2-D tensor tiles) of the FP32 lattice
+update against per-thread cp.async staging (0): the same arithmetic on the
+same data, so they must agree bit for bit.  The lattices cover every alignment of the halo rows the bulk copies move
 (x extent odd and even, x*y extent 0..3 modulo 4, so rows start 0..3 values
 before a 16-byte boundary), tiles shorter than one x-row, and the arena's
 first and last cells (rows that begin before the arena or end after it are
@@ -36,11 +37,12 @@ def _run(bulk, tile, steps):
                 [sim.status(c) for c in range(len(cells))])
 
 
+@pytest.mark.parametrize("staging", [1, 2])
 @pytest.mark.parametrize("tile", [64, 128, 256])
-def test_bulk_staging_equals_per_thread_staging(tile):
+def test_bulk_staging_equals_per_thread_staging(tile, staging):
     steps = 4400  # through the first upstroke, 44 output steps
     a = _run(0, tile, steps)
-    b = _run(1, tile, steps)
+    b = _run(staging, tile, steps)
     assert b[3] == a[3]
     for c in range(len(a[0])):
         assert b[1][c] == a[1][c], c
