@@ -232,9 +232,9 @@ def main():
     ap.add_argument("--persistent", type=int, default=0, choices=[0, 1],
                     help="with --tile: 1 = one persistent launch per window, 0 = two "
                          "launches per step and cell group")
-    ap.add_argument("--bulk", type=int, default=0, choices=[0, 1],
+    ap.add_argument("--bulk", type=int, default=0, choices=[0, 1, 2],
                     help="with --tile, two-launch path, mixed precision: 1 = staging by bulk "
-                         "asynchronous copies")
+                         "asynchronous copies, 2 = by tensor copies")
     args = ap.parse_args()
     rank, world, local = _env_rank()
     if args.impl == "reference":
