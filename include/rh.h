@@ -353,14 +353,16 @@ int rh_set_launch_shape(rh_sim* sim, const rh_launch_shape* shape);
 /* Launch-shape autotuner.  Times `steps` lattice updates of the live
  * workload with every candidate shape (persistent launches with tiles of 64
  * and 128 at both CTA counts; two-launch windows with tiles of 64, 128 and
- * 256 at 8, 16 and 24 cell groups, in mixed precision with either staging),
+ * 256 at 8, 12, 16 and 24 cell groups, in mixed precision with each staging),
  * each from a device-side copy of the
  * current state that is restored afterwards (the simulation does not
  * advance), and switches to the fastest.  The choice is cached for the
  * process by device, precision and lattice classes (the cells' interior x
  * and y extents in steps of 16 and their CRU total): a later simulator of
  * the same workload on the same device reuses it without timing (then
- * *ntried = 0).  tried/ms_per_step (max_tried entries each, may be NULL)
+ * *ntried = 0).  With the environment variable RH_SHAPE_CACHE naming a
+ * file, choices are also appended to it and read from it, so that later
+ * processes reuse them too.  tried/ms_per_step (max_tried entries each, may be NULL)
  * receive the candidates and their ms per lattice update of every cell. */
 int rh_autotune_shapes(rh_sim* sim, int32_t steps, rh_launch_shape* best,
                        rh_launch_shape* tried, double* ms_per_step, int32_t max_tried,

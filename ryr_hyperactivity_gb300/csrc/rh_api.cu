@@ -11,6 +11,7 @@
 #include <stdarg.h>
 #include <stddef.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -1788,6 +1789,46 @@ std::string workload_key(const rh_sim* s) {
   return k;
 }
 
+// The file that keeps choices across processes (environment RH_SHAPE_CACHE),
+// one line per choice: key, tab, persistent tile fewer groups staging; the
+// last line of a key counts.
+const char* shape_cache_file() {
+  const char* p = getenv("RH_SHAPE_CACHE");
+  return (p && *p) ? p : nullptr;
+}
+
+bool shape_file_lookup(const std::string& key, rh_launch_shape& out) {
+  const char* path = shape_cache_file();
+  if (!path) return false;
+  FILE* f = fopen(path, "r");
+  if (!f) return false;
+  bool found = false;
+  char line[4096];
+  while (fgets(line, sizeof(line), f)) {
+    char* tab = strchr(line, '\t');
+    if (!tab || (size_t)(tab - line) != key.size() || key.compare(0, key.size(), line, key.size()))
+      continue;
+    rh_launch_shape sh{};
+    if (sscanf(tab + 1, "%d %d %d %d %d", &sh.persistent, &sh.tile_crus, &sh.fewer_ctas,
+               &sh.cell_groups, &sh.bulk_staging) == 5) {
+      out = sh;
+      found = true;
+    }
+  }
+  fclose(f);
+  return found;
+}
+
+void shape_file_store(const std::string& key, const rh_launch_shape& sh) {
+  const char* path = shape_cache_file();
+  if (!path) return;
+  FILE* f = fopen(path, "a");
+  if (!f) return;
+  fprintf(f, "%s\t%d %d %d %d %d\n", key.c_str(), sh.persistent, sh.tile_crus, sh.fewer_ctas,
+          sh.cell_groups, sh.bulk_staging);
+  fclose(f);
+}
+
 }  // namespace
 
 int rh_autotune_shapes(rh_sim* s, int32_t steps, rh_launch_shape* best,
@@ -1801,11 +1842,19 @@ int rh_autotune_shapes(rh_sim* s, int32_t steps, rh_launch_shape* best,
   {
     std::lock_guard<std::mutex> lock(g_shape_mu);
     auto it = g_shape_cache.find(key);
-    if (it != g_shape_cache.end()) {
-      const rh_launch_shape cached = it->second;
+    rh_launch_shape cached{};
+    bool hit = it != g_shape_cache.end();
+    if (hit) cached = it->second;
+    else if (shape_file_lookup(key, cached)) hit = true;
+    if (hit) {
       int r = rh_set_launch_shape(s, &cached);
-      if (r == RH_OK && best) *best = cached;
-      return r;
+      if (r == RH_OK) {
+        g_shape_cache[key] = cached;
+        if (best) *best = cached;
+        return r;
+      }
+      // a stored shape this build cannot run: time the candidates instead
+      g_shape_cache.erase(key);
     }
   }
   // candidates
@@ -1893,6 +1942,7 @@ int rh_autotune_shapes(rh_sim* s, int32_t steps, rh_launch_shape* best,
   {
     std::lock_guard<std::mutex> lock(g_shape_mu);
     g_shape_cache[key] = win;
+    shape_file_store(key, win);
   }
   if (best) *best = win;
   CK(cudaGetLastError());

@@ -154,3 +154,27 @@ def test_wait_that_never_completes_times_out_and_leaves_the_gpu_usable():
     b = _run(cells, "fp64", 1, [120])
     for c in range(len(cells)):
         assert b["membrane"][c] == a["membrane"][c]
+
+
+def test_shape_choice_persists_across_processes(tmp_path):
+    """With RH_SHAPE_CACHE set, the autotuner's choice is written to that file
+    and a new process takes it from there without timing."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from ryr_hyperactivity_gb300.sim import Simulator\n"
+            "from ryr_hyperactivity_gb300.workloads import config3_cells\n"
+            "sim = Simulator(config3_cells(512)[:4], precision='mixed', record_linescan=0)\n"
+            "sim.run_steps(20)\n"
+            "best, tried = sim.autotune_shapes(4)\n"
+            "print(len(tried), best['persistent'], best['tile_crus'], best['cell_groups'],"
+            " best['bulk_staging'])\n" % root)
+    env = dict(os.environ, RH_SHAPE_CACHE=str(tmp_path / "shapes.txt"))
+    first = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                           check=True).stdout.split()
+    assert int(first[0]) > 0 and (tmp_path / "shapes.txt").exists()
+    second = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True,
+                            text=True, check=True).stdout.split()
+    assert second[0] == "0" and second[1:] == first[1:]
